@@ -1,0 +1,73 @@
+"""Generate the golden fixtures in tests/golden/ by running pi-qmc's own code.
+
+Runs oracle/_ref/libpimcref.so (pi-qmc's hot-path sources, built from the
+reference tree by oracle/build_ref.py) on seeded synthetic inputs and stores:
+the configuration, the initial path, the pair-action and Ewald tables the
+reference built, per-attempt records (section start, moving particle, rejecting
+level, per-level action differences and mover log transition ratios), the
+final path (stored as its difference from the initial path, which compresses)
+and the thermodynamic energy estimator of the final path.
+
+The fixtures let machines without the reference tree (the GPU machine) pin the C++
+restatement and the CUDA engine against the reference's own outputs.
+
+Usage: python tests/golden/make_golden.py   (needs the reference tree)
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+import oracle_lib as O  # noqa: E402
+import workloads as W  # noqa: E402
+
+
+def run_case(name, kw, init, nattempt):
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    x0 = W.initial_path(cfg, init)
+    ref.set_path(x0)
+    tabs = ref.pair_tables()
+    ew = ref.ewald_table()
+    e0 = ref.thermo_energy()
+    recs = ref.run(nattempt)
+    x1 = ref.get_path()
+    e1 = ref.thermo_energy()
+    out = dict(
+        config=np.array(repr(kw)), init=np.array(init), nattempt=nattempt,
+        path0=x0, dpath=x1 - x0, energy0=e0, energy1=e1,
+        npair=len(tabs),
+    )
+    for k, t in enumerate(tabs):
+        s1, s2 = O.species_pair_of(t, cfg)
+        out[f"pair{k}_species"] = np.array([s1, s2], np.int32)
+        out[f"pair{k}_grid"] = np.array([t["ngpts"], t["norder"]], np.int32)
+        out[f"pair{k}_params"] = np.array([t["rgridinv"], t["logrratioinv"]])
+        out[f"pair{k}_ugrid"] = t["ugrid"]
+    if ew is not None:
+        out["ewald_kvec"] = ew["kvec"]
+        out["ewald_vk"] = ew["vk"]
+        out["ewald_scalars"] = np.array([ew["one_over_2v"], ew["self_energy"]])
+        out["ewald_ikmax"] = np.array(ew["ikmax"], np.int32)
+        out["ewald_coef"] = ew["coef"]
+    for k in ("ifirst1", "ifirst2", "ipart", "reject_level", "ds", "ds_node", "lnt"):
+        out["rec_" + k] = recs[k]
+    out["naccepted"] = recs["naccepted"]
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {nattempt} attempts, {recs['naccepted']} accepted, "
+          f"E={e1:.6f}, {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main():
+    for name, (kw, init, n) in W.GOLDEN_CASES.items():
+        run_case(name, kw, init, n)
+
+
+if __name__ == "__main__":
+    main()

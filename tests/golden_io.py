@@ -1,0 +1,31 @@
+"""Loading helpers for the golden fixtures made by tests/golden/make_golden.py."""
+import ast
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    kw = ast.literal_eval(str(z["config"]))
+    tabs = []
+    for k in range(int(z["npair"])):
+        g = z[f"pair{k}_grid"]
+        p = z[f"pair{k}_params"]
+        tabs.append(dict(species=tuple(int(v) for v in z[f"pair{k}_species"]),
+                         ngpts=int(g[0]), norder=int(g[1]), rgridinv=float(p[0]),
+                         logrratioinv=float(p[1]), ugrid=z[f"pair{k}_ugrid"]))
+    ew = None
+    if "ewald_kvec" in z:
+        ew = dict(totk=len(z["ewald_vk"]), kvec=z["ewald_kvec"], vk=z["ewald_vk"],
+                  one_over_2v=float(z["ewald_scalars"][0]),
+                  self_energy=float(z["ewald_scalars"][1]),
+                  ikmax=[int(v) for v in z["ewald_ikmax"]], coef=z["ewald_coef"])
+    rec = {k: z["rec_" + k] for k in ("ifirst1", "ifirst2", "ipart", "reject_level", "ds",
+                                      "ds_node", "lnt")}
+    return dict(kw=kw, tables=tabs, ewald=ew, path0=z["path0"],
+                path1=z["path0"] + z["dpath"], energy0=float(z["energy0"]),
+                energy1=float(z["energy1"]), records=rec, nattempt=int(z["nattempt"]),
+                naccepted=int(z["naccepted"]))

@@ -1,0 +1,146 @@
+"""The CPU checkers: the restatement (oracle/port.cc) pinned against pi-qmc's
+own unit-test known answers, the golden fixtures made by pi-qmc's own code,
+and (where the reference tree is present) oracle/_ref directly."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import golden_io
+import oracle_lib as O
+import workloads as W
+
+# Tolerances.  Plain action differences and mover ratios: 1e-12 relative.
+# Node-model differences: 1e-10 relative for well-conditioned Slater matrices;
+# dot20_fn (omega/T = 20) has Slater matrices with condition numbers ~1e9, where
+# two correct LU orderings (OpenBLAS vs this one) differ at ~1e-3 relative in the
+# nodal action, so that case is held to 1e-2 relative and exact decisions.
+NODE_TOL = {"dot20_fn": 1e-2}
+
+
+def rel_close(a, b, tol, floor=1.0):
+    return np.all(np.abs(a - b) <= tol * np.maximum(np.abs(a), floor))
+
+
+def port_for(case):
+    g = golden_io.load(case)
+    cfg = O.make_config(**g["kw"])
+    return g, cfg, O.PortOracle(cfg, g["tables"], g["ewald"])
+
+
+# ---- reference unit-test known answers -----------------------------------
+def _lib():
+    return O.PortOracle.lib()
+
+
+def test_sho_action_known_answer():
+    # unit-tests/action/SHOActionTest.cc:62-70: one bead of 64 moved to (1,2,3).
+    cfg = O.make_config(counts=[1], sho_omega=[1.0], nslice=64, beta=6.4, nlevel=6,
+                        spring=0, cell=10.0)
+    sec = np.zeros((65, 1, 3))
+    mov = np.zeros((65, 1, 3))
+    assert O.PortOracle(cfg).action_diff(0, sec, mov, 0) == 0.0
+    mov[32, 0] = [1, 2, 3]
+    d = O.PortOracle(cfg).action_diff(0, sec, mov, 0)
+    assert np.float32(d) == pytest.approx(np.float32(0.46635586), rel=4 * 2.0 ** -23)
+
+
+@pytest.mark.parametrize("a,b", [(0.5, 0.0), (0.5, 1.0)])
+def test_prim_sho_known_answer(a, b):
+    # unit-tests/action/PrimSHOActionTest.cc:56-79: (a r^2 + b r^4) tau.
+    cfg = O.make_config(counts=[1], prim_a=[a], prim_b=[b], nslice=64, beta=6.4,
+                        nlevel=6, spring=0, cell=10.0)
+    sec = np.zeros((65, 1, 3))
+    mov = np.zeros((65, 1, 3))
+    mov[32, 0] = [1, 2, 3]
+    r2 = 14.0
+    d = O.PortOracle(cfg).action_diff(0, sec, mov, 0)
+    assert np.float32(d) == pytest.approx(np.float32((a * r2 + b * r2 * r2) * 0.1),
+                                          rel=4 * 2.0 ** -23)
+
+
+def test_periodic_gaussian_known_answers():
+    # unit-tests/util/PeriodicGaussianTest.cc:24-92 (alpha=2.5, L=1.5).
+    L = _lib()
+    L.port_pg_terms.restype = C.c_int
+    L.port_pg_terms.argtypes = [C.c_double, C.c_double]
+    L.port_pg_eval.restype = C.c_double
+    L.port_pg_eval.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]
+    assert L.port_pg_terms(2.5, 1.5) == 5
+    assert L.port_pg_terms(2.5, 20.0) == 64
+    g = C.c_double()
+    for x, v, dv in [(0.0, 1.0072131266104112, 0.0),
+                     (0.4999 * 1.5, 0.49012750361989998, -0.00066637454689608252),
+                     (-0.3 * 1.5, 0.66635569537953232, 1.0233852136355668)]:
+        val = L.port_pg_eval(2.5, 1.5, x, C.byref(g))
+        assert val == pytest.approx(v, rel=4e-16, abs=0)
+        assert g.value == pytest.approx(dv, rel=1e-14, abs=1e-15)
+
+
+def test_supercell_pbc_known_answer():
+    # unit-tests/util/SuperCellTest.cc:12-32.
+    L = _lib()
+    L.port_pbc.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    a = (C.c_double * 3)(1, 2, 4)
+    v = (C.c_double * 3)(0.1, 2, 2.5)
+    L.port_pbc(a, v)
+    assert list(v) == [0.1, 0.0, -1.5]
+
+
+# ---- golden fixtures from pi-qmc's own code ---------------------------------
+@pytest.mark.parametrize("case", list(W.GOLDEN_CASES))
+def test_port_matches_golden(case):
+    g, cfg, port = port_for(case)
+    port.set_path(g["path0"])
+    assert port.thermo_energy() == pytest.approx(g["energy0"], rel=1e-12)
+    r = port.run(g["nattempt"])
+    ref = g["records"]
+    for k in ("ifirst1", "ifirst2", "ipart", "reject_level"):
+        assert np.array_equal(r[k], ref[k]), k
+    assert r["naccepted"] == g["naccepted"]
+    assert rel_close(r["ds"], ref["ds"], 1e-12)
+    assert rel_close(r["lnt"], ref["lnt"], 1e-12)
+    assert rel_close(r["ds_node"], ref["ds_node"], NODE_TOL.get(case, 1e-10))
+    assert np.abs(port.get_path() - g["path1"]).max() <= 1e-12
+    assert port.thermo_energy() == pytest.approx(g["energy1"], rel=1e-12)
+
+
+# ---- direct comparison with the reference build (where it exists) ---------
+needs_ref = pytest.mark.skipif(not O.RefOracle.available(),
+                               reason="oracle/_ref not built (no reference tree)")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_port_matches_reference_dot(seed):
+    kw = W.dot2(nslice=128, seed=seed)
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    port = O.PortOracle(cfg, ref.pair_tables(), ref.ewald_table())
+    x = W.initial_path(cfg, "gauss", seed=seed)
+    ref.set_path(x)
+    port.set_path(x)
+    a, b = ref.run(500), port.run(500)
+    for k in ("ifirst1", "ipart", "reject_level"):
+        assert np.array_equal(a[k], b[k])
+    assert rel_close(a["ds"], b["ds"], 1e-12)
+    assert np.array_equal(ref.get_path(), port.get_path())
+
+
+@needs_ref
+def test_port_matches_reference_action_levels():
+    # Action-level parity at every level on random sections (FakeSampler).
+    kw = W.dot20_fn(counts=[3, 2], nslice=64, nlevel=4, node_kind=[0, 0])
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    port = O.PortOracle(cfg, ref.pair_tables(), None)
+    rng = np.random.default_rng(5)
+    for trial in range(20):
+        sec = rng.normal(size=(17, 5, 3))
+        ip = int(rng.integers(5))
+        mov = sec[:, ip, :].copy()
+        mov[1:-1] += 0.3 * rng.normal(size=(15, 3))
+        for level in range(5):
+            a = ref.action_diff(level, sec, mov, ip)
+            b = port.action_diff(level, sec, mov, ip)
+            assert abs(a - b) <= 1e-12 * max(abs(a), 1.0)
