@@ -1,0 +1,222 @@
+/* pimc_gb300 — C ABI of the GB300 (sm_103a) path-integral Monte Carlo engine.
+ *
+ * The engine runs pi-qmc's multilevel-bisection hot path on the GPU: the
+ * action difference of a bisection move (kinetic spring, harmonic and
+ * primitive confinement, tabulated Coulomb pair action with Ewald long-range
+ * term), the fixed-node Slater-determinant check on every changed slice with
+ * the nodal action, the free-particle bisection mover, the section choosers,
+ * and the thermodynamic energy estimator.  Each entry point below names the
+ * pi-qmc interface it replaces (file:line in the reference tree).
+ *
+ * Conventions
+ *  - Every function returns PIMC_OK (0) or a negative PIMC_ERR_* code; the
+ *    message of the last failure is available from pimc_last_error().  Nothing
+ *    here calls exit(): pi-qmc's exit-on-error paths
+ *    (src/fixednode/SHONodes.cc:86-111, src/fixednode/FixedNodeAction.cc:342-349)
+ *    become per-replica status words (pimc_replica_status).
+ *  - Host arrays are caller-owned and plain C; device memory is owned by the
+ *    engine.  Paths are [replica][slice][particle][xyz] doubles, i.e. pi-qmc's
+ *    Beads storage (src/base/Beads.h:131-225) with slices outermost.
+ *  - Work is issued on the stream set by pimc_set_stream (default: the legacy
+ *    default stream); calls that return host data synchronize that stream.
+ */
+#ifndef PIMC_GB300_H
+#define PIMC_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIMC_MAX_SPECIES 4
+#define PIMC_MAX_LEVEL 6
+#define PIMC_MAX_NODE_PARTICLES 32
+
+enum {
+  PIMC_OK = 0,
+  PIMC_ERR_INVALID = -1,     /* bad argument or unsupported configuration */
+  PIMC_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+  PIMC_ERR_NO_DEVICE = -3,   /* no sm_103a device */
+  PIMC_ERR_CAPACITY = -4     /* a size beyond a documented maximum */
+};
+
+/* Node models (src/fixednode/SHONodes.h, src/fixednode/FreeParticleNodes.h). */
+enum { PIMC_NODES_NONE = 0, PIMC_NODES_SHO = 1, PIMC_NODES_FREE = 2 };
+/* Bisection movers (src/advancer/mover/FreeMover.h, FreeMoverPBC.h). */
+enum { PIMC_MOVER_FREE = 0, PIMC_MOVER_FREE_PBC = 1 };
+/* Arithmetic of the move kernels. */
+enum {
+  PIMC_PREC_FP64 = 0,  /* everything in FP64: the plain form, parity with pi-qmc */
+  PIMC_PREC_MIXED = 1  /* FP32 spring/pair sums with compensated accumulation;
+                          FP64 determinants, sign tests, Ewald phases, totals */
+};
+
+/* One simulated system: what pi-qmc's SimulationInfo (src/base/SimulationInfo.h)
+ * plus the action/sampler XML attributes describe.  Species occupy consecutive
+ * particle ranges in order. */
+typedef struct {
+  int npart;
+  int nspecies;
+  int spec_count[PIMC_MAX_SPECIES];
+  double spec_mass[PIMC_MAX_SPECIES];
+  double spec_charge[PIMC_MAX_SPECIES];
+  double sho_omega[PIMC_MAX_SPECIES];  /* >0: SHOAction on the species */
+  double prim_a[PIMC_MAX_SPECIES];     /* PrimSHOAction a x^2 + b x^4 */
+  double prim_b[PIMC_MAX_SPECIES];
+  int node_kind[PIMC_MAX_SPECIES];     /* PIMC_NODES_* per species */
+  double node_omega[PIMC_MAX_SPECIES];
+  double node_temperature;             /* trial density-matrix temperature */
+  int nslice;
+  double tau;
+  int nlevel;                          /* sections hold 2^nlevel + 1 slices */
+  double cell[3];
+  int spring;                          /* SpringAction on */
+  int coulomb;                         /* CoulombAction on (needs pair tables) */
+  double epsilon;
+  int ewald;                           /* long-range Ewald term (needs an Ewald table) */
+  int mover;                           /* PIMC_MOVER_* */
+} pimc_system;
+
+/* A tabulated pair action, pi-qmc's PairAction::ugrid(ngpts,2,norder+1) on a
+ * logarithmic grid (src/action/PairAction.cc:161-185,601-655), row-major
+ * (index (i*2+t)*(norder+1)+k; t=0 action, t=1 tau derivative). */
+typedef struct {
+  int species1, species2;
+  int ngpts, norder;
+  double rgridinv, logrratioinv;
+  const double* ugrid;
+} pimc_pair_table;
+
+/* Long-range Ewald data of an EwaldSum (src/util/EwaldSum.h:60-134): half-space
+ * k-vectors (integer multiples of 2pi/L), their v_k, 1/(2V), self energy. */
+typedef struct {
+  int totk;
+  const int* kvec; /* totk x 3 */
+  const double* vk;
+  double one_over_2v;
+  double self_energy;
+  int ikmax[3];
+} pimc_ewald_table;
+
+/* One attempted section move (for parity checks and statistics). */
+typedef struct {
+  int ifirst1, ifirst2;  /* section starts; ifirst2 = -2 without fixed node */
+  int ipart;             /* moving particle */
+  int reject_level;      /* level that rejected, -1 when accepted */
+  double ds[PIMC_MAX_LEVEL + 3];       /* Action difference per level */
+  double ds_node[PIMC_MAX_LEVEL + 3];  /* DoubleAction difference per level */
+  double lnt[PIMC_MAX_LEVEL + 3];      /* mover ln(T_old/T_new) per level */
+} pimc_move_record;
+
+/* Per-replica status word bits. */
+enum {
+  PIMC_STATUS_INIT_CROSSING = 1,  /* node crossing found when a section was set up */
+  PIMC_STATUS_SINGULAR = 2,       /* a Slater matrix had an exactly zero pivot */
+  PIMC_STATUS_RESCALE_LIMIT = 4,  /* determinant rescaling hit its iteration limit */
+  PIMC_STATUS_NONFINITE = 8       /* a non-finite bead coordinate was seen */
+};
+
+typedef struct pimc_engine pimc_engine;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Creates an engine holding nreplica copies of one system, each with its own
+ * path and random stream (replica r draws stream r of the seed).  Replaces the
+ * object graph pi-qmc's parsers build for one clone
+ * (src/parser/ActionParser.cc:105-153,433-452, src/parser/PIMCParser.cc:312-491):
+ * SpringAction, SHOAction, PrimSHOAction, CoulombAction (from the given pair
+ * tables and Ewald table), FixedNodeAction with SHONodes/FreeParticleNodes,
+ * FreeMover/FreeMoverPBC, SectionChooser or DoubleSectionChooser, and a
+ * MultiLevelSampler/DoubleMLSampler moving one particle chosen by
+ * SimpleParticleChooser. */
+int pimc_engine_create(const pimc_system* sys, int nreplica, const pimc_pair_table* tables,
+                       int ntables, const pimc_ewald_table* ewald, uint64_t seed,
+                       int precision, pimc_engine** out);
+
+/* Creates an engine whose replicas are different systems (uneven particle
+ * counts, slice counts, levels, frequencies): the batched form.  sys[r] is
+ * replica r's system; table_offset[r]..table_offset[r+1] index its pair tables. */
+int pimc_engine_create_batch(const pimc_system* sys, int nreplica,
+                             const pimc_pair_table* tables, const int* table_offset,
+                             uint64_t seed, int precision, pimc_engine** out);
+
+int pimc_engine_destroy(pimc_engine* e);
+const char* pimc_last_error(void);
+/* cudaStream_t to issue work on (NULL: legacy default stream). */
+int pimc_set_stream(pimc_engine* e, void* stream);
+
+/* ---- paths (SerialPaths::getBeads/putBeads, src/base/SerialPaths.cc:119-185) */
+
+/* Host <-> device copies of all replicas' paths (host layout above). */
+int pimc_upload_paths(pimc_engine* e, const double* host_xyz);
+int pimc_download_paths(pimc_engine* e, double* host_xyz);
+/* Offsets (in doubles) of each replica's path in the packed host layout; for
+ * engines of one system this is r * nslice * npart * 3. */
+int pimc_path_offsets(pimc_engine* e, int64_t* offsets /* nreplica+1 */);
+
+/* ---- the sampler ------------------------------------------------------- */
+
+/* Runs nattempt section-move attempts on every replica, on the device, in
+ * pi-qmc's order: SectionChooser::run (src/advancer/SectionChooser.cc:30-48) or
+ * DoubleSectionChooser::run (src/advancer/DoubleSectionChooser.cc:33-65) around
+ * MultiLevelSampler::tryMove (src/advancer/MultiLevelSampler.cc:100-177) or
+ * DoubleMLSampler::tryMove (src/advancer/DoubleMLSampler.cc:123-245).
+ * Asynchronous on the engine's stream.  records (optional, host) receives
+ * nreplica*nattempt records, replica-major; requesting them synchronizes. */
+int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records);
+
+/* Per-replica accepted-move counts and status words since creation. */
+int pimc_replica_status(pimc_engine* e, int64_t* accepted, int64_t* attempted,
+                        uint32_t* status);
+
+/* ---- estimators -------------------------------------------------------- */
+
+/* Thermodynamic energy estimator of every replica's current path:
+ * (1/M) sum over links of utau, as ThermoEnergyEstimator::handleLink
+ * (src/estimator/ThermoEnergyEstimator.cc:32-50) summing
+ * CompositeAction::getBeadAction (src/action/CompositeAction.cc:59-69). */
+int pimc_thermo_energy(pimc_engine* e, double* host_energy /* nreplica */);
+
+/* ---- Action-level entry point ----------------------------------------- */
+
+/* Action::getActionDifference(const SectionSamplerInterface&, int level)
+ * (src/action/Action.h:44, src/action/CompositeAction.cc:30-37) for nbatch
+ * independent sections of replica 0's system: section[b] is
+ * [2^nlevel+1][npart][3], moving[b] is [2^nlevel+1][3] for particle ipart[b].
+ * Returns the composite difference (spring + SHO + PrimSHO + Coulomb, Ewald at
+ * level 0) per batch entry in ds[b]. Host arrays; synchronous. */
+int pimc_action_difference(pimc_engine* e, int level, int nbatch, const double* section,
+                           const double* moving, const int* ipart, double* ds);
+
+/* ---- NodeModel-level entry point --------------------------------------- */
+
+/* NodeModel::evaluate + evaluateDistance (src/fixednode/NodeModel.h:74-90,
+ * src/fixednode/SHONodes.cc:51-170, src/fixednode/FreeParticleNodes.cc:72-234)
+ * for species ispec of replica 0's system on nbatch slice pairs: r1[b], r2[b]
+ * are [npart][3].  det[b] gets the Slater determinant (at the engine's current
+ * scale for that species, no rescaling), d1[b]/d2[b] ([npart]) the nodal
+ * distances (200 for particles of other species), err[b] 1 for a singular
+ * matrix.  Host arrays; synchronous. */
+int pimc_node_evaluate(pimc_engine* e, int ispec, int nbatch, const double* r1,
+                       const double* r2, double* det, double* d1, double* d2, int* err);
+int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale);
+
+/* ---- random streams ---------------------------------------------------- */
+
+/* The first n uniforms and n normals of replica `replica`'s attempt `attempt`
+ * (the numbers the sampler consumes in place of pi-qmc's RandomNumGenerator,
+ * src/util/RandomNumGenerator.h:41-85), generated on the device; lets a CPU
+ * replay check it consumes bit-identical numbers.  Synchronous. */
+int pimc_stream_sample(uint64_t seed, uint32_t replica, uint32_t attempt, int n,
+                       double* uniforms, double* normals);
+
+/* ---- timing ------------------------------------------------------------ */
+
+/* Kernel launches issued by this engine so far (for launch accounting). */
+int64_t pimc_kernel_launches(pimc_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -106,6 +106,17 @@ def build_port(force=False):
     return PORT_LIB
 
 
+def cpu_stream(seed, replica, attempt, n):
+    """Uniforms and normals of one attempt's streams, computed on the CPU."""
+    L = PortOracle.lib()
+    L.port_stream_sample.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_int,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    u = np.zeros(n)
+    z = np.zeros(n)
+    L.port_stream_sample(C.c_uint64(seed), replica, attempt, n, _dp(u), _dp(z))
+    return u, z
+
+
 def records_to_numpy(recs, n):
     out = {
         "ifirst1": np.array([recs[i].ifirst1 for i in range(n)], np.int32),

@@ -1195,6 +1195,15 @@ double port_ewald_long_range(void* h, const double* r) {
   return s->ewald.evalLongRange(rv);
 }
 
+// The replayed random streams (CPU side of the bit-exactness check).
+void port_stream_sample(uint64_t seed, uint32_t replica, uint32_t attempt, int n, double* u,
+                        double* z) {
+  for (int i = 0; i < n; ++i) {
+    u[i] = pimc::stream_uniform(seed, replica, attempt, (uint32_t)i);
+    z[i] = pimc::stream_normal(seed, replica, attempt, (uint32_t)i);
+  }
+}
+
 // Pieces exposed for the reference unit-test known answers.
 int port_pg_terms(double alpha, double length) { return PGauss::numberOfTerms(alpha, length); }
 double port_pg_eval(double alpha, double length, double x, double* grad) {

@@ -1,0 +1,723 @@
+// Kernels: the section-move sampler, the thermodynamic energy estimator, and
+// the Action-/NodeModel-level entry points.
+#pragma once
+#include "../../include/pimc_gb300.h"
+#include "section_kernel.cuh"
+
+namespace pimc {
+
+// Offsets (in doubles) of the shared-memory working set; computed on the host
+// for the largest replica of a launch.
+struct Layout {
+  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl;
+  int nodescr_in_smem;
+  int nodescr_stride;
+  int total;  // doubles
+};
+
+struct RunParams {
+  const DevSys* sys;
+  DevState* state;
+  double* paths;
+  double* nodescr_g;  // global per-warp node scratch when it does not fit in smem
+  pimc_move_record* rec;
+  int nattempt;
+  int nrep;
+  uint64_t seed;
+  Layout lay;
+};
+
+__device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSys& s,
+                                      double* nodescr_g) {
+  Smem m;
+  const int ss = s.nsec * s.npart;
+  m.s1x = base + L.s1;
+  m.s1y = m.s1x + ss;
+  m.s1z = m.s1y + ss;
+  m.s2x = base + L.s2;
+  m.s2y = m.s2x + ss;
+  m.s2z = m.s2y + ss;
+  m.mx = base + L.mv;
+  m.my = m.mx + s.nsec;
+  m.mz = m.my + s.nsec;
+  m.red = base + L.red;
+  m.qpart = base + L.q;
+  m.dm = base + L.dm;
+  m.ndm = base + L.ndm;
+  m.edet = base + L.edet;
+  m.dist = base + L.dist;
+  m.ndist = base + L.ndist;
+  m.ewt = base + L.ewt;
+  m.ictl = (int*)(base + L.ictl);
+  m.nodescr_stride = L.nodescr_stride;
+  m.nodescr = L.nodescr_in_smem
+                  ? base + L.nodescr
+                  : nodescr_g + (size_t)blockIdx.x * kWarps * L.nodescr_stride;
+  return m;
+}
+
+__device__ __forceinline__ int species_of(const DevSys& s, int p) {
+  int r = 0;
+  for (int k = 0; k < s.nspecies; ++k)
+    if (p >= s.spec_first[k] && p < s.spec_first[k] + s.spec_count[k]) r = k;
+  return r;
+}
+
+// Section slice k of a section starting at ifirst, in path slice numbering with
+// the identity permutation (SerialPaths::getBeads, src/base/SerialPaths.cc:119-136).
+__device__ __forceinline__ int wrap_slice(int islice, int M) {
+  return islice < 0 ? islice + M : (islice < M ? islice : islice - M);
+}
+
+__device__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
+                             double* sy, double* sz) {
+  const int np = s.npart, n = s.nsec * np;
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const int k = idx / np, p = idx - k * np;
+    const int t = wrap_slice(ifirst + k, s.nslice);
+    const double* src = path + ((size_t)t * np + p) * 3;
+    sx[idx] = src[0];
+    sy[idx] = src[1];
+    sz[idx] = src[2];
+  }
+}
+
+// SerialPaths::putBeads (src/base/SerialPaths.cc:143-185) with the identity permutation.
+__device__ void store_section(const DevSys& s, double* path, int ifirst, const double* sx,
+                              const double* sy, const double* sz) {
+  const int np = s.npart, n = s.nsec * np;
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const int k = idx / np, p = idx - k * np;
+    const int islice = ifirst + k;
+    if (islice < 0) continue;
+    const int t = islice < s.nslice ? islice : islice % s.nslice;
+    double* dst = path + ((size_t)t * np + p) * 3;
+    dst[0] = sx[idx];
+    dst[1] = sy[idx];
+    dst[2] = sz[idx];
+  }
+}
+
+// FreeMover::makeMove (src/advancer/mover/FreeMover.cc:59-124) and
+// FreeMoverPBC::makeMove (src/advancer/mover/FreeMoverPBC.cc:59-152) for one
+// moving particle at one level; threads own moved slices.  Returns ln(T_old/T_new).
+__device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
+                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
+  const int L = s.nlevel, np = s.npart;
+  const int nStride = 1 << level;
+  const int nmov = (level == L) ? 0 : (1 << (L - level - 1));
+  const int ord0 = (level == L) ? 0 : (1 << (L - level - 1)) - 1;
+  const int sp = species_of(s, ipart);
+  const double sigma = 1.0 * sqrt(s.lambda[sp] * s.tau * nStride);
+  const double inv2Sigma2 = 0.5 / (sigma * sigma);
+  double part = 0.0;
+  for (int k = threadIdx.x; k < nmov; k += blockDim.x) {
+    const int t = nStride * (2 * k + 1), tp = t - nStride, tn = t + nStride;
+    double z0, z1, z2, z3;
+    stream_normal_pair(seed, rep, att, 2u * (ord0 + k), &z0, &z1);
+    stream_normal_pair(seed, rep, att, 2u * (ord0 + k) + 1u, &z2, &z3);
+    const double ox = m.s1x[t * np + ipart], oy = m.s1y[t * np + ipart], oz = m.s1z[t * np + ipart];
+    const double opx = m.s1x[tp * np + ipart], opy = m.s1y[tp * np + ipart], opz = m.s1z[tp * np + ipart];
+    const double onx = m.s1x[tn * np + ipart], ony = m.s1y[tn * np + ipart], onz = m.s1z[tn * np + ipart];
+    const double mpx = m.mx[tp], mpy = m.my[tp], mpz = m.mz[tp];
+    const double mnx = m.mx[tn], mny = m.my[tn], mnz = m.mz[tn];
+    double acc = 0.0;
+    if (s.mover == PIMC_MOVER_FREE) {
+      double mdx = mnx - mpx, mdy = mny - mpy, mdz = mnz - mpz;
+      pbc(s, mdx, mdy, mdz);
+      mdx *= 0.5; mdy *= 0.5; mdz *= 0.5;
+      mdx += mpx; mdy += mpy; mdz += mpz;
+      pbc(s, mdx, mdy, mdz);
+      double dx = z0 * sigma, dy = z1 * sigma, dz = z2 * sigma;
+      pbc(s, dx, dy, dz);
+      double nx = mdx + dx, ny = mdy + dy, nz = mdz + dz;
+      pbc(s, nx, ny, nz);
+      m.mx[t] = nx;
+      m.my[t] = ny;
+      m.mz[t] = nz;
+      acc += dx * dx * inv2Sigma2;
+      acc += dy * dy * inv2Sigma2;
+      acc += dz * dz * inv2Sigma2;
+      double ax = onx - opx, ay = ony - opy, az = onz - opz;
+      pbc(s, ax, ay, az);
+      ax *= 0.5; ay *= 0.5; az *= 0.5;
+      ax += opx; ay += opy; az += opz;
+      pbc(s, ax, ay, az);
+      double ex = ox - ax, ey = oy - ay, ez = oz - az;
+      pbc(s, ex, ey, ez);
+      acc -= ex * ex * inv2Sigma2;
+      acc -= ey * ey * inv2Sigma2;
+      acc -= ez * ez * inv2Sigma2;
+    } else {
+      double md[3] = {mnx - mpx, mny - mpy, mnz - mpz};
+      pbc(s, md[0], md[1], md[2]);
+      md[0] *= 0.5; md[1] *= 0.5; md[2] *= 0.5;
+      double m2[3] = {md[0] + 0.5 * s.cell[0], md[1] + 0.5 * s.cell[1], md[2] + 0.5 * s.cell[2]};
+      pbc(s, m2[0], m2[1], m2[2]);
+      for (int d = 0; d < 3; ++d) {
+        // No periodic Gaussian on the mover path (the engine rejects boxes that need one).
+        const double w1 = exp(-inv2Sigma2 * md[d] * md[d]);
+        const double w2 = exp(-inv2Sigma2 * m2[d] * m2[d]);
+        const double u = stream_uniform(seed, rep, att, ubase + 3u * k + d);
+        if (u > w1 / (w1 + w2)) md[d] = m2[d];
+      }
+      double nx = md[0] + mpx + z0 * sigma, ny = md[1] + mpy + z1 * sigma, nz = md[2] + mpz + z2 * sigma;
+      pbc(s, nx, ny, nz);
+      m.mx[t] = nx;
+      m.my[t] = ny;
+      m.mz[t] = nz;
+      double pn[3] = {nx - mpx, ny - mpy, nz - mpz}, nn[3] = {nx - mnx, ny - mny, nz - mnz};
+      double dn[3] = {mnx - mpx, mny - mpy, mnz - mpz};
+      double po[3] = {ox - opx, oy - opy, oz - opz}, no[3] = {ox - onx, oy - ony, oz - onz};
+      double dol[3] = {onx - opx, ony - opy, onz - opz};
+      pbc(s, pn[0], pn[1], pn[2]);
+      pbc(s, nn[0], nn[1], nn[2]);
+      pbc(s, dn[0], dn[1], dn[2]);
+      pbc(s, po[0], po[1], po[2]);
+      pbc(s, no[0], no[1], no[2]);
+      pbc(s, dol[0], dol[1], dol[2]);
+      for (int d = 0; d < 3; ++d) {
+        acc -= po[d] * po[d] * inv2Sigma2 * 0.5;
+        acc -= no[d] * no[d] * inv2Sigma2 * 0.5;
+        acc += pn[d] * pn[d] * inv2Sigma2 * 0.5;
+        acc += nn[d] * nn[d] * inv2Sigma2 * 0.5;
+        acc += dol[d] * dol[d] * inv2Sigma2 * 0.25;
+        acc -= dn[d] * dn[d] * inv2Sigma2 * 0.25;
+      }
+    }
+    part += acc;
+  }
+  return block_sum(part, m.red);
+}
+
+// FixedNodeAction::initialize (src/fixednode/FixedNodeAction.cc:331-357) for every
+// species with a node model, reproducing NodeModel::evaluate's rescaling loop
+// (src/fixednode/SHONodes.cc:112-126): slices are evaluated in parallel at the
+// current scale; at the first slice whose determinant leaves [1e-50, 1e50] the
+// loop is replayed sequentially, and later slices are re-evaluated.
+__device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int msp,
+                                uint32_t* status) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nsec = s.nsec;
+  const int nsm = s.ns_max;
+  int* errs = m.ictl + C_NCTL;  // [nsec]
+  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride;
+  for (int sp = 0; sp < s.nspecies; ++sp) {
+    if (!s.node_kind[sp]) continue;
+    const int full = sp == msp;
+    int start = 0;
+    for (int round = 0; round < 64; ++round) {
+      const double sc = scale[sp];
+      for (int t = start + warp; t < nsec; t += kWarps) {
+        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
+        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
+        double det;
+        int err;
+        node_eval_warp(s, sp, v1, v2, sc, scr, full, det, err, m.dist + (t * 2) * nsm,
+                       m.dist + (t * 2 + 1) * nsm);
+        if (lane == 0) {
+          m.edet[t] = det;
+          errs[t] = err;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int k = -1;
+        for (int t = start; t < nsec; ++t) {
+          const double a = fabs(m.edet[t]);
+          if (errs[t] || a < 1e-50 || a > 1e50) {
+            k = t;
+            break;
+          }
+        }
+        m.ictl[C_SCANK] = k;
+      }
+      __syncthreads();
+      const int k = m.ictl[C_SCANK];
+      if (k < 0) break;
+      if (warp == 0) {
+        double det = m.edet[k];
+        int err = errs[k];
+        double sc2 = scale[sp];
+        int guard = 0;
+        while (err || fabs(det) < 1e-50 || fabs(det) > 1e50) {
+          if (err || ++guard > 2000) {
+            if (lane == 0) *status |= err ? (PIMC_STATUS_SINGULAR | PIMC_STATUS_RESCALE_LIMIT)
+                                          : PIMC_STATUS_RESCALE_LIMIT;
+            break;
+          }
+          if (fabs(det) < 1e-250)
+            sc2 *= 2;
+          else
+            sc2 *= pow(fabs(det), -1. / s.spec_count[sp]);
+          SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, k, -1, 0, 0, 0};
+          SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, k, -1, 0, 0, 0};
+          node_eval_warp(s, sp, v1, v2, sc2, scr, full, det, err, m.dist + (k * 2) * nsm,
+                         m.dist + (k * 2 + 1) * nsm);
+        }
+        if (lane == 0) {
+          m.edet[k] = det;
+          errs[k] = err;
+          scale[sp] = sc2;
+        }
+      }
+      __syncthreads();
+      start = k + 1;
+      if (start >= nsec) break;
+    }
+    // crossing check, as the reference counts errors at set-up
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < nsec; ++t) {
+        m.dm[sp * nsec + t] = m.edet[t];
+        if (errs[t] || m.edet[t] * m.edet[0] <= 1e-200) *status |= PIMC_STATUS_INIT_CROSSING;
+      }
+    }
+    __syncthreads();
+  }
+  if (msp >= 0 && s.node_kind[msp]) {
+    // newDist(0) = dist(0)
+    for (int i = threadIdx.x; i < 2 * nsm; i += blockDim.x) m.ndist[i] = m.dist[i];
+  }
+  __syncthreads();
+}
+
+// FixedNodeAction::getActionDifference (src/fixednode/FixedNodeAction.cc:39-131)
+// for the moving species at one level.
+__device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
+                             int level) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nsec = s.nsec, nsm = s.ns_max;
+  const int nStride = 1 << (level + 1);
+  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride;
+  if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
+  __syncthreads();
+  const int ntask = (nsec - 1 - nStride / 2) / nStride + 1;
+  for (int task = warp; task < ntask; task += kWarps) {
+    const int t = nStride / 2 + task * nStride;
+    SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
+    SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
+    double det;
+    int err;
+    node_eval_warp(s, msp, v1, v2, scale, scr, 1, det, err, m.ndist + (t * 2) * nsm,
+                   m.ndist + (t * 2 + 1) * nsm);
+    if (lane == 0) {
+      m.ndm[t] = det;
+      if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
+    }
+  }
+  __syncthreads();
+  if (m.ictl[C_FLAG]) return 2e100;
+  if (level != 0) return 0.0;
+  const int n = s.spec_count[msp];
+  double part = 0.0;
+  for (int it = threadIdx.x; it < (nsec - 1) * n; it += blockDim.x) {
+    const int t = 1 + it / n, p = it % n;
+    const double* D0 = m.dist + (t * 2) * nsm;
+    const double* Dp0 = m.dist + ((t - 1) * 2) * nsm;
+    const double* N0 = m.ndist + (t * 2) * nsm;
+    const double* Np0 = m.ndist + ((t - 1) * 2) * nsm;
+    double a = log((1 - exp(-D0[p] * Dp0[p])) / (1 - exp(-N0[p] * Np0[p])));
+    a += log((1 - exp(-D0[nsm + p] * Dp0[nsm + p])) / (1 - exp(-N0[nsm + p] * Np0[nsm + p])));
+    part += a;
+  }
+  return block_sum(part, m.red);
+}
+
+// The uniform-stream index of the first uniform consumed at `level`
+// (image choices of FreeMoverPBC, then the Metropolis uniform).
+__device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int level) {
+  uint32_t u = (s.fixed_node ? 2u : 1u) + 1u;  // section choice + particle choice
+  const uint32_t pbcu = s.mover == PIMC_MOVER_FREE_PBC ? 3u : 0u;
+  for (int l = s.nlevel; l > level; --l) {
+    const uint32_t nmov = (l == s.nlevel) ? 0u : (1u << (s.nlevel - l - 1));
+    u += pbcu * nmov + 1u;
+  }
+  return u;
+}
+
+__global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  __shared__ double scale[kMaxSpecies];
+  __shared__ uint32_t status;
+  __shared__ long long nacc;
+  for (int r = blockIdx.x; r < P.nrep; r += gridDim.x) {
+    {
+      const int* src = (const int*)(P.sys + r);
+      int* dst = (int*)&S;
+      for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+        dst[i] = src[i];
+    }
+    if (threadIdx.x == 0) {
+      status = P.state[r].status;
+      nacc = 0;
+      for (int k = 0; k < kMaxSpecies; ++k) scale[k] = P.state[r].node_scale[k];
+    }
+    __syncthreads();
+    const DevSys& s = S;
+    Smem m = carve(smem, P.lay, s, P.nodescr_g);
+    double* path = P.paths + s.path_offset;
+    const uint32_t att0 = P.state[r].attempt;
+    const int np = s.npart, nsec = s.nsec, M = s.nslice, L = s.nlevel;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
+    for (int a = 0; a < P.nattempt; ++a) {
+      const uint32_t att = att0 + (uint32_t)a;
+      // ---- section choice and moving particle
+      if (threadIdx.x == 0) {
+        int i1, i2 = -2;
+        uint32_t ui = 0;
+        const double x = stream_uniform(P.seed, r, att, ui++) * (1 - 1e-8);
+        if (!s.fixed_node) {
+          const int ilo = -1, ihi = M - 1;
+          i1 = ilo + (int)((ihi + 1 - ilo) * x);
+          if (i1 > ihi) i1 = ihi;
+        } else {
+          const int ilo = -1, ihi = M / 2 - 1;
+          i1 = ilo + (int)((ihi + 1 - ilo) * x);
+          if (i1 > ihi) i1 = ihi;
+          if (stream_uniform(P.seed, r, att, ui++) >= 0.5) i1 = (i1 + M / 2 + 1) % M - 1;
+          i2 = (i1 + M / 2 + 1) % M - 1;
+        }
+        int ip = (int)(np * stream_uniform(P.seed, r, att, ui++));
+        if (ip >= np) ip = np - 1;
+        m.ictl[C_IFIRST1] = i1;
+        m.ictl[C_IFIRST2] = i2;
+        m.ictl[C_IPART] = ip;
+        m.ictl[C_REJECT] = -1;
+      }
+      __syncthreads();
+      const int ifirst1 = m.ictl[C_IFIRST1], ifirst2 = m.ictl[C_IFIRST2];
+      const int ipart = m.ictl[C_IPART];
+      load_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
+      if (s.fixed_node) load_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+      __syncthreads();
+      for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
+        m.mx[t] = m.s1x[t * np + ipart];
+        m.my[t] = m.s1y[t * np + ipart];
+        m.mz[t] = m.s1z[t * np + ipart];
+      }
+      const int msp = species_of(s, ipart);
+      const bool mynode = s.fixed_node && s.node_kind[msp];
+      if (s.fixed_node) node_initialize(s, m, scale, mynode ? msp : -1, &status);
+      __syncthreads();
+      pimc_move_record* rec = P.rec ? P.rec + (size_t)r * P.nattempt + a : nullptr;
+      double oldDS = 0.0;
+      int reject = -1;
+      for (int level = L; level >= 0; --level) {
+        const uint32_t ubase = level_uniform_base(s, level);
+        const double lnT = mover_level(s, m, ipart, level, P.seed, r, att, ubase);
+        double ds = block_sum(action_partial(s, m, ipart, level), m.red);
+        if (s.ewald && s.coulomb && level == 0) {
+          for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
+        }
+        double dsn = 0.0;
+        if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level);
+        if (threadIdx.x == 0) {
+          const double total = s.fixed_node ? ds + dsn : ds;
+          const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
+          const uint32_t uacc =
+              ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
+          const double p = exp(lnT + (-total + oldDS));
+          const double u = stream_uniform(P.seed, r, att, uacc);
+          if (rec) {
+            rec->ds[level] = ds;
+            rec->ds_node[level] = dsn;
+            rec->lnt[level] = lnT;
+          }
+          if (!(isfinite(lnT) && isfinite(ds))) status |= PIMC_STATUS_NONFINITE;
+          if (u > p) m.ictl[C_REJECT] = level;
+          m.red[kWarps + 2] = total;
+        }
+        __syncthreads();
+        reject = m.ictl[C_REJECT];
+        if (reject >= 0) break;
+        oldDS = m.red[kWarps + 2];
+      }
+      if (reject < 0) {
+        for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
+          m.s1x[t * np + ipart] = m.mx[t];
+          m.s1y[t * np + ipart] = m.my[t];
+          m.s1z[t * np + ipart] = m.mz[t];
+        }
+        if (threadIdx.x == 0) ++nacc;
+      }
+      if (threadIdx.x == 0 && rec) {
+        rec->ifirst1 = ifirst1;
+        rec->ifirst2 = ifirst2;
+        rec->ipart = ipart;
+        rec->reject_level = reject;
+      }
+      __syncthreads();
+      // SerialPaths::putDoubleBeads order (src/base/SerialPaths.cc:187-205).
+      if (!s.fixed_node || ifirst1 < M / 2 - 1) {
+        store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
+        if (s.fixed_node) {
+          __syncthreads();
+          store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+        }
+      } else {
+        store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+        __syncthreads();
+        store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      P.state[r].attempt = att0 + (uint32_t)P.nattempt;
+      P.state[r].status = status;
+      P.state[r].accepted += nacc;
+      P.state[r].attempted += P.nattempt;
+      for (int k = 0; k < kMaxSpecies; ++k) P.state[r].node_scale[k] = scale[k];
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ estimator
+// utau of one link (ipart, islice) summed over the composite action, as
+// CompositeAction::getBeadAction feeds ThermoEnergyEstimator::handleLink:
+// SpringAction (src/action/SpringAction.cc:112-123), SHOAction
+// (src/action/SHOAction.cc:71-105), PrimSHOAction (src/action/PrimSHOAction.cc:66-81),
+// PairAction (src/action/PairAction.cc:509-599).  The Ewald term is added per slice.
+__device__ double link_utau(const DevSys& s, const double* path, int ip, int t) {
+  const int np = s.npart, M = s.nslice;
+  const int tm = t == 0 ? M - 1 : t - 1;
+  const double* b1 = path + ((size_t)t * np + ip) * 3;
+  const double* b0 = path + ((size_t)tm * np + ip) * 3;
+  const int sp = species_of(s, ip);
+  const double tau = s.tau;
+  double utau = 0.0;
+  double dx = b1[0] - b0[0], dy = b1[1] - b0[1], dz = b1[2] - b0[2];
+  pbc(s, dx, dy, dz);
+  if (s.spring) utau += 3 / (2 * tau) - dot3(dx, dy, dz, dx, dy, dz) / (4.0 * s.lambda[sp] * tau * tau);
+  const double om = s.sho_omega[sp];
+  if (om > 0) {
+    const double m = s.mass[sp];
+    const double wt = om * tau, sinhwt = sinh(wt), coshwt = cosh(wt);
+    const double cschwt = 1.0 / sinhwt, cothwt = coshwt * cschwt, tin = 1.0 / tau;
+    const double r0r0 = b0[0] * b0[0] + b0[1] * b0[1] + b0[2] * b0[2];
+    const double r1r1 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
+    const double r0r1 = b0[0] * b1[0] + b0[1] * b1[1] + b0[2] * b1[2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    utau += 0.5 * 3 * om * cothwt +
+            0.5 * m * om * om *
+                ((r1r1 + r0r0) * (1 - cothwt * cothwt) + 2.0 * r0r1 * coshwt * cschwt * cschwt) +
+            0.5 * m * d2 * tin * tin - 0.5 * 3 * tin;
+  }
+  if (s.prim_a[sp] != 0 || s.prim_b[sp] != 0) {
+    const double x2 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
+    utau += s.prim_a[sp] * x2 + s.prim_b[sp] * x2 * x2;
+  }
+  if (s.coulomb) {
+    double uc = 0.0;
+    for (int ti = 0; ti < s.ntab; ++ti) {
+      const DevTable& tb = s.tab[ti];
+      int jb, je;
+      if (ip >= tb.ifirst1 && ip < tb.ifirst1 + tb.npart1) {
+        jb = tb.ifirst2;
+        je = tb.ifirst2 + tb.npart2;
+      } else if (ip >= tb.ifirst2 && ip < tb.ifirst2 + tb.npart2) {
+        jb = tb.ifirst1;
+        je = tb.ifirst1 + tb.npart1;
+      } else {
+        continue;
+      }
+      double up = 0.0;
+      for (int j = jb; j < je; ++j) {
+        if (j == ip) continue;
+        const double* c1 = path + ((size_t)t * np + j) * 3;
+        const double* c0 = path + ((size_t)tm * np + j) * 3;
+        double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
+        pbc(s, ex, ey, ez);
+        double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
+        pbc(s, px, py, pz);
+        const double r = sqrt(dot3(ex, ey, ez, ex, ey, ez));
+        const double rp = sqrt(dot3(px, py, pz, px, py, pz));
+        const double q = 0.5 * (r + rp);
+        const double sx = ex - px, sy = ey - py, sz = ez - pz;
+        const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (q * q);
+        double v, vt;
+        tab_uk0d(tb, q, s2, v, vt);
+        up += 0.5 * vt;
+      }
+      uc += up;
+    }
+    utau += uc;
+  }
+  return utau;
+}
+
+struct ThermoParams {
+  const DevSys* sys;
+  const double* paths;
+  double* partial;  // [nrep][nchunk]
+  int nchunk;
+  int nrep;
+  Layout lay;
+};
+
+// One CTA per (chunk of slices, replica): link utau sums plus, for Coulomb with
+// Ewald, the long-range energy of each slice (CoulombAction::getBeadAction adds
+// it at ipart == 0, src/action/CoulombAction.cc:165-171).
+__global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  const int r = blockIdx.y;
+  {
+    const int* src = (const int*)(P.sys + r);
+    int* dst = (int*)&S;
+    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  const DevSys& s = S;
+  const double* path = P.paths + s.path_offset;
+  const int M = s.nslice, np = s.npart;
+  const int per = (M + P.nchunk - 1) / P.nchunk;
+  const int t0 = blockIdx.x * per, t1 = min(M, t0 + per);
+  Smem m = carve(smem, P.lay, s, nullptr);
+  double part = 0.0;
+  for (int it = threadIdx.x; it < (t1 - t0) * np; it += blockDim.x) {
+    const int t = t0 + it / np, ip = it % np;
+    part += link_utau(s, path, ip, t);
+  }
+  double tot = block_sum(part, m.red);
+  if (s.coulomb && s.ewald) {
+    for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
+    for (int t = t0; t < t1; ++t) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        const double* b = path + ((size_t)t * np + i) * 3;
+        m.s1x[i] = b[0];
+        m.s1y[i] = b[1];
+        m.s1z[i] = b[2];
+      }
+      if (threadIdx.x == 0) {
+        m.mx[0] = m.s1x[0];
+        m.my[0] = m.s1y[0];
+        m.mz[0] = m.s1z[0];
+      }
+      __syncthreads();
+      // ipart = 0 with the moved bead equal to the old one: new sum == old sum.
+      const double d = ewald_slice_energy(s, m, 0);
+      tot += d / s.epsilon;
+    }
+  }
+  if (threadIdx.x == 0) P.partial[(size_t)r * P.nchunk + blockIdx.x] = tot;
+}
+
+// ------------------------------------------------------- Action-level entry
+struct ActionDiffParams {
+  const DevSys* sys;
+  const double* section;  // [nbatch][nsec][npart][3]
+  const double* moving;   // [nbatch][nsec][3]
+  const int* ipart;
+  double* ds;
+  int level;
+  Layout lay;
+};
+
+__global__ void __launch_bounds__(kBlock) action_diff_kernel(ActionDiffParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  {
+    const int* src = (const int*)(P.sys);
+    int* dst = (int*)&S;
+    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  const DevSys& s = S;
+  Smem m = carve(smem, P.lay, s, nullptr);
+  const int b = blockIdx.x, np = s.npart, nsec = s.nsec;
+  const double* sec = P.section + (size_t)b * nsec * np * 3;
+  const double* mov = P.moving + (size_t)b * nsec * 3;
+  for (int idx = threadIdx.x; idx < nsec * np; idx += blockDim.x) {
+    m.s1x[idx] = sec[idx * 3];
+    m.s1y[idx] = sec[idx * 3 + 1];
+    m.s1z[idx] = sec[idx * 3 + 2];
+  }
+  for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
+    m.mx[t] = mov[t * 3];
+    m.my[t] = mov[t * 3 + 1];
+    m.mz[t] = mov[t * 3 + 2];
+  }
+  for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
+  __syncthreads();
+  const int ip = P.ipart[b];
+  double ds = block_sum(action_partial(s, m, ip, P.level), m.red);
+  if (s.ewald && s.coulomb && P.level == 0)
+    for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ip, t);
+  if (threadIdx.x == 0) P.ds[b] = ds;
+}
+
+// ---------------------------------------------------- NodeModel-level entry
+struct NodeEvalParams {
+  const DevSys* sys;
+  const DevState* state;
+  const double* r1;  // [nbatch][npart][3]
+  const double* r2;
+  double* det;
+  double* d1;  // [nbatch][npart]
+  double* d2;
+  int* err;
+  int ispec;
+  Layout lay;
+};
+
+__global__ void __launch_bounds__(kBlock) node_eval_kernel(NodeEvalParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  {
+    const int* src = (const int*)(P.sys);
+    int* dst = (int*)&S;
+    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  const DevSys& s = S;
+  const int np = s.npart, b = blockIdx.x, sp = P.ispec;
+  double* sx = smem;
+  double* sy = sx + 2 * np;
+  double* sz = sy + 2 * np;
+  double* dd = sz + 2 * np;  // [2][np]
+  double* scr = dd + 2 * np;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    sx[i] = P.r1[((size_t)b * np + i) * 3];
+    sy[i] = P.r1[((size_t)b * np + i) * 3 + 1];
+    sz[i] = P.r1[((size_t)b * np + i) * 3 + 2];
+    sx[np + i] = P.r2[((size_t)b * np + i) * 3];
+    sy[np + i] = P.r2[((size_t)b * np + i) * 3 + 1];
+    sz[np + i] = P.r2[((size_t)b * np + i) * 3 + 2];
+    dd[i] = 200;
+    dd[np + i] = 200;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    SliceView v1{sx, sy, sz, np, 0, -1, 0, 0, 0};
+    SliceView v2{sx, sy, sz, np, 1, -1, 0, 0, 0};
+    double det;
+    int err;
+    const int f = s.spec_first[sp];
+    node_eval_warp(s, sp, v1, v2, P.state[0].node_scale[sp], scr, 1, det, err, dd + f, dd + np + f);
+    if (threadIdx.x == 0) {
+      P.det[b] = det;
+      P.err[b] = err;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    P.d1[(size_t)b * np + i] = dd[i];
+    P.d2[(size_t)b * np + i] = dd[np + i];
+  }
+}
+
+__global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, int n, double* u,
+                                     double* z) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  u[i] = stream_uniform(seed, rep, att, (uint32_t)i);
+  z[i] = stream_normal(seed, rep, att, (uint32_t)i);
+}
+
+}  // namespace pimc

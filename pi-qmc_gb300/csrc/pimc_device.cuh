@@ -1,0 +1,200 @@
+// Device-side data structures and physics for the bisection hot path.
+// Each function cites the pi-qmc routine whose arithmetic it follows.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pimc_rng.h"
+
+namespace pimc {
+
+constexpr int kMaxSpecies = 4;
+constexpr int kMaxTables = 10;
+constexpr int kMaxNs = 32;  // particles per node-model species
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+
+struct DevTable {
+  const double* ugrid;  // (ngpts,2,ndata)
+  const float* ugrid32; // same table in FP32 (mixed precision)
+  int ngpts, norder, ndata, s1, s2;
+  int ifirst1, npart1, ifirst2, npart2;
+  double rgridinv, logrratioinv;
+};
+
+struct DevSys {
+  int npart, nspecies, nslice, nlevel, nsec;
+  int spec_first[kMaxSpecies], spec_count[kMaxSpecies];
+  double mass[kMaxSpecies], lambda[kMaxSpecies], charge[kMaxSpecies];
+  double sho_omega[kMaxSpecies], prim_a[kMaxSpecies], prim_b[kMaxSpecies];
+  int node_kind[kMaxSpecies];
+  double node_c[kMaxSpecies], node_cosh[kMaxSpecies];  // SHONodes constants
+  // FreeParticleNodes: PeriodicGaussian(alpha = m T, L) per species and axis.
+  double pg_nome[kMaxSpecies][3], pg_pref[kMaxSpecies][3], pg_k[kMaxSpecies][3];
+  int pg_nmax[kMaxSpecies][3];
+  double tau;
+  double cell[3], cellb[3], rcut2;
+  int spring, coulomb, ewald, mover, fixed_node;
+  double epsilon;
+  int ntab;
+  DevTable tab[kMaxTables];
+  int totk;
+  const int* kvec;
+  const double* vk;
+  double one_over_2v, self_energy, deltak[3];
+  int ikmax[3];
+  int ns_max;           // largest node-species count
+  long long path_offset;  // doubles into the path pool
+  long long inv_offset;   // doubles into the node scratch pool (-1: shared memory)
+};
+
+// Mutable per-replica state kept on the device between launches.
+struct DevState {
+  uint32_t attempt;
+  uint32_t status;
+  long long accepted;
+  long long attempted;
+  double node_scale[kMaxSpecies];
+};
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by,
+                                       double bz) {
+  // (a0 b0 + a1 b1) + a2 b2 without contraction, as blitz::dot evaluates it.
+  return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+
+// SuperCell::pbc (src/util/SuperCell.cc:25-34): minimum image, only applied
+// when |v|^2 exceeds a quarter of the shortest side squared.
+__device__ __forceinline__ void pbc(const DevSys& s, double& x, double& y, double& z) {
+  if (dot3(x, y, z, x, y, z) > s.rcut2) {
+    const double ix = floor(__dadd_rn(__dmul_rn(s.cellb[0], x), 1000.5)) - 1000;
+    const double iy = floor(__dadd_rn(__dmul_rn(s.cellb[1], y), 1000.5)) - 1000;
+    const double iz = floor(__dadd_rn(__dmul_rn(s.cellb[2], z), 1000.5)) - 1000;
+    x = __dsub_rn(x, __dmul_rn(s.cell[0], ix));
+    y = __dsub_rn(y, __dmul_rn(s.cell[1], iy));
+    z = __dsub_rn(z, __dmul_rn(s.cell[2], iz));
+  }
+}
+
+// PeriodicGaussian::evaluate (src/util/PeriodicGaussian.cc:20-40): theta series
+// value and gradient.
+__device__ __forceinline__ double pg_eval(double nome, double pref, double k, int nmax, double x,
+                                          double* grad) {
+  double sw, cw;
+  sincos(k * x, &sw, &cw);
+  double tr = 1.0, ti = 0.0;  // term
+  double s0r = 0.0, s1r = 0.0;
+  double nomeN = 1.0;
+  for (int n = 1; n < nmax; ++n) {
+    const double f = nomeN * nomeN * nome;
+    const double fr = f * cw, fi = f * sw;
+    const double nr = tr * fr - ti * fi;
+    const double ni = tr * fi + ti * fr;
+    tr = nr;
+    ti = ni;
+    s0r += tr;
+    s1r += (-ti * k) * double(n);  // real(term * i k * n)
+    nomeN *= nome;
+  }
+  *grad = pref * 2 * s1r;
+  return pref * (1 + 2 * s0r);
+}
+
+// Pair-action table lookup on the logarithmic grid
+// (PairAction::u00 / uk0 / uk0CalcDerivatives, src/action/PairAction.cc:601-655).
+__device__ __forceinline__ void tab_locate(const DevTable& t, double q, int& i, double& x) {
+  q *= t.rgridinv;
+  x = log(q) * t.logrratioinv;
+  i = (int)x;
+  if (q < 1) {
+    i = 0;
+    x = 0;
+  } else if (i > t.ngpts - 2) {
+    i = t.ngpts - 2;
+    x = 1;
+  } else {
+    x -= i;
+  }
+}
+
+__device__ __forceinline__ double tab_u00(const DevTable& t, double r) {
+  int i;
+  double x;
+  tab_locate(t, r, i, x);
+  const double* g = t.ugrid + (size_t)i * 2 * t.ndata;
+  return (1 - x) * __ldg(g) + x * __ldg(g + 2 * t.ndata);
+}
+
+__device__ __forceinline__ double tab_uk0(const DevTable& t, double q, double s2) {
+  int i;
+  double x;
+  tab_locate(t, q, i, x);
+  const double* g0 = t.ugrid + (size_t)i * 2 * t.ndata;
+  const double* g1 = g0 + 2 * t.ndata;
+  double a = 0;
+  for (int k = t.norder; k >= 0; k--) a = a * s2 + ((1 - x) * __ldg(g0 + k) + x * __ldg(g1 + k));
+  return a;
+}
+
+__device__ __forceinline__ void tab_uk0d(const DevTable& t, double q, double s2, double& u,
+                                         double& ut) {
+  int i;
+  double x;
+  tab_locate(t, q, i, x);
+  const double* g0 = t.ugrid + (size_t)i * 2 * t.ndata;
+  const double* g1 = g0 + 2 * t.ndata;
+  u = 0;
+  ut = 0;
+  for (int k = t.norder; k >= 0; k--) {
+    u = u * s2 + ((1 - x) * __ldg(g0 + k) + x * __ldg(g1 + k));
+    ut = ut * s2 + ((1 - x) * __ldg(g0 + t.ndata + k) + x * __ldg(g1 + t.ndata + k));
+  }
+}
+
+// FP32 variants for the mixed-precision form (same grid, FP32 coefficients).
+__device__ __forceinline__ float tab_uk0_f(const DevTable& t, float q, float s2, int norder_eff) {
+  q *= (float)t.rgridinv;
+  float x = __logf(q) * (float)t.logrratioinv;
+  int i = (int)x;
+  if (q < 1.f) {
+    i = 0;
+    x = 0.f;
+  } else if (i > t.ngpts - 2) {
+    i = t.ngpts - 2;
+    x = 1.f;
+  } else {
+    x -= i;
+  }
+  const float* g0 = t.ugrid32 + (size_t)i * 2 * t.ndata;
+  const float* g1 = g0 + 2 * t.ndata;
+  float a = 0.f;
+  for (int k = norder_eff; k >= 0; k--) a = fmaf(a, s2, fmaf(x, __ldg(g1 + k) - __ldg(g0 + k), __ldg(g0 + k)));
+  return a;
+}
+
+// Error-free sum of two doubles (Knuth TwoSum) for compensated accumulation.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Deterministic block sum of one double per thread (fixed tree order).
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < kWarps) ? red[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (l == 0) red[kWarps] = v;
+  }
+  __syncthreads();
+  return red[kWarps];
+}
+
+}  // namespace pimc

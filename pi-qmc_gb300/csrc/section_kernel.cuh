@@ -1,0 +1,537 @@
+// The bisection section-move kernel: one CTA advances one replica through a
+// sequence of section-move attempts, entirely on the device.
+//
+// Per attempt (pi-qmc order, SURVEY call stacks CS1/CS2):
+//   SectionChooser::run / DoubleSectionChooser::run   -> choose section(s), stage in smem
+//   FixedNodeAction::initialize                        -> det + distances on every slice
+//   SimpleParticleChooser::chooseParticles             -> moving particle
+//   MultiLevelSampler::tryMove / DoubleMLSampler::tryMove, levels L..0:
+//       FreeMover(PBC)::makeMove, CompositeAction::getActionDifference,
+//       FixedNodeAction::getActionDifference, Metropolis test
+//   SerialPaths::putBeads / putDoubleBeads             -> section(s) back to HBM
+//
+// Random numbers come from the counter-addressed streams of pimc_rng.h, so the
+// CPU checkers can replay exactly the numbers a replica consumed.
+#pragma once
+#include "pimc_device.cuh"
+
+namespace pimc {
+
+// Shared-memory working set of one CTA (carved from dynamic shared memory).
+struct Smem {
+  double *s1x, *s1y, *s1z;  // section 1: [nsec][npart]
+  double *s2x, *s2y, *s2z;  // section 2 (fixed node)
+  double *mx, *my, *mz;     // moving beads [nsec]
+  double* red;              // reduction scratch
+  double* dm;               // [nspecies][nsec] determinants at section set-up
+  double* ndm;              // [nsec] determinants of the moving species' new slices
+  double* dist;             // [nsec][2][ns_max] distances at set-up (moving species)
+  double* ndist;            // [nsec][2][ns_max] distances of the new path
+  double* edet;             // [nsec] speculative determinants during set-up
+  double* ewt;              // Ewald exp(ik.r) tables for one slice
+  double* qpart;            // [npart] charges
+  int* ictl;                // control words
+  double* nodescr;          // per-warp node scratch (smem or global)
+  int nodescr_stride;       // doubles per warp
+};
+
+enum {
+  C_IFIRST1 = 0, C_IFIRST2, C_IPART, C_REJECT, C_FLAG, C_SCANK, C_ERRS, C_NCTL = 16
+};
+
+struct SectionSizes {
+  // all counts in doubles
+  static __host__ __device__ long long section(int nsec, int npart) { return 3LL * nsec * npart; }
+};
+
+// Positions of particle p on section slice t, with the moving bead substituted.
+struct SliceView {
+  const double *sx, *sy, *sz;
+  int npart;
+  int t;
+  int imov;  // substituted particle or -1
+  double mxv, myv, mzv;
+  __device__ __forceinline__ void get(int p, double& x, double& y, double& z) const {
+    if (p == imov) {
+      x = mxv;
+      y = myv;
+      z = mzv;
+    } else {
+      const int o = t * npart + p;
+      x = sx[o];
+      y = sy[o];
+      z = sz[o];
+    }
+  }
+};
+
+// ------------------------------------------------------------------ node model
+// NodeModel::evaluate (+ evaluateDistance) for one species on one slice pair,
+// executed by one warp.  Lanes own matrix rows.  LU with partial pivoting
+// (first largest |pivot|, LAPACK dgetrf semantics), determinant from the U
+// diagonal and pivots, inverse by solving A X = I column per lane (dgetri
+// semantics), then the log-gradient nodal distances
+// (src/fixednode/SHONodes.cc:51-170, src/fixednode/FreeParticleNodes.cc:72-234).
+// full = 0: determinant only.
+__device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, const SliceView& v2,
+                               double scale, double* scr, int full, double& det_out,
+                               int& err_out, double* d1, double* d2) {
+  const int lane = threadIdx.x & 31;
+  const int n = s.spec_count[sp];
+  const int f = s.spec_first[sp];
+  double* A = scr;          // n*n column-major, LU then scratch
+  double* X = scr + n * n;  // n*n inverse, column-major
+  double* E = X + n * n;    // n*n exp values (SHO nodes)
+  const bool sho = s.node_kind[sp] == 1;
+  // --- build the Slater matrix: A(i,j) = scale * rho(r1_j, r2_i)
+  if (lane < n) {
+    double rix, riy, riz;
+    v2.get(f + lane, rix, riy, riz);
+    if (sho) {
+      const double c = s.node_c[sp], ch = s.node_cosh[sp];
+      const double ri2 = dot3(rix, riy, riz, rix, riy, riz);
+      for (int j = 0; j < n; ++j) {
+        double rjx, rjy, rjz;
+        v1.get(f + j, rjx, rjy, rjz);
+        const double rj2 = dot3(rjx, rjy, rjz, rjx, rjy, rjz);
+        const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
+        const double e = exp(-c * ((ri2 + rj2) * ch - 2.0 * rirj));
+        E[j * n + lane] = e;
+        A[j * n + lane] = scale * e;
+      }
+    } else {
+      for (int j = 0; j < n; ++j) {
+        double rjx, rjy, rjz;
+        v1.get(f + j, rjx, rjy, rjz);
+        double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
+        pbc(s, dx, dy, dz);
+        double g, ear2 = scale;
+        ear2 *= pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g);
+        ear2 *= pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g);
+        ear2 *= pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g);
+        A[j * n + lane] = ear2;
+      }
+    }
+  }
+  __syncwarp();
+  // --- LU with partial pivoting
+  int info = 0;
+  unsigned pivbits = 0;  // bit j set: row j was interchanged
+  int piv_lane = lane;   // piv[lane] for lane < n
+  for (int j = 0; j < n; ++j) {
+    double av = (lane >= j && lane < n) ? fabs(A[j * n + lane]) : -1.0;
+    int ai = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_down_sync(0xffffffffu, av, o);
+      const int oi = __shfl_down_sync(0xffffffffu, ai, o);
+      if (ov > av || (ov == av && oi < ai)) {
+        av = ov;
+        ai = oi;
+      }
+    }
+    const int p = __shfl_sync(0xffffffffu, ai, 0);
+    if (lane == j) piv_lane = p;
+    const double apj = A[j * n + p];
+    if (apj != 0.0) {
+      if (p != j) {
+        pivbits |= 1u << j;
+        for (int k = lane; k < n; k += 32) {
+          const double t = A[k * n + j];
+          A[k * n + j] = A[k * n + p];
+          A[k * n + p] = t;
+        }
+      }
+      __syncwarp();
+      const double rinv = 1.0 / A[j * n + j];
+      if (lane > j && lane < n) A[j * n + lane] *= rinv;
+    } else if (info == 0) {
+      info = j + 1;
+    }
+    __syncwarp();
+    if (lane > j && lane < n) {
+      const double lij = A[j * n + lane];
+      for (int k = j + 1; k < n; ++k) A[k * n + lane] -= lij * A[k * n + j];
+    }
+    __syncwarp();
+  }
+  // --- determinant (sequential product, as the reference)
+  double det = 1.0;
+  for (int i = 0; i < n; ++i) {
+    det *= A[i * n + i];
+    det *= ((pivbits >> i) & 1u) ? -1 : 1;
+  }
+  det_out = det;
+  err_out = info != 0;
+  if (!full || info != 0) return;
+  // --- inverse: lane c solves A x = e_c
+  int pos = lane;  // e_c after the row interchanges (every lane takes part in the shuffles)
+  for (int j = 0; j < n; ++j) {
+    const int pj = __shfl_sync(0xffffffffu, piv_lane, j);
+    if (pos == j)
+      pos = pj;
+    else if (pos == pj)
+      pos = j;
+  }
+  if (lane < n) {
+    double* x = X + lane * n;
+    for (int i = 0; i < n; ++i) x[i] = (i == pos) ? 1.0 : 0.0;
+    for (int j = pos; j < n; ++j) {
+      const double xj = x[j];
+      for (int i = j + 1; i < n; ++i) x[i] -= A[j * n + i] * xj;
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      const double xj = x[j] / A[j * n + j];
+      x[j] = xj;
+      for (int i = 0; i < j; ++i) x[i] -= A[j * n + i] * xj;
+    }
+  }
+  __syncwarp();
+  // --- nodal distances.  inv(j,i) = X[i*n + j].
+  const double twom_tau = 2 * s.mass[sp];
+  if (lane < n) {
+    const int j = lane;  // d1: gradient with respect to r1_j
+    double rjx, rjy, rjz;
+    v1.get(f + j, rjx, rjy, rjz);
+    double lx = 0, ly = 0, lz = 0;
+    for (int i = 0; i < n; ++i) {
+      double rix, riy, riz;
+      v2.get(f + i, rix, riy, riz);
+      double gx, gy, gz;
+      if (sho) {
+        const double c = s.node_c[sp], ch = s.node_cosh[sp];
+        const double e = E[j * n + i];
+        gx = 2 * c * (rix - ch * rjx) * e;
+        gy = 2 * c * (riy - ch * rjy) * e;
+        gz = 2 * c * (riz - ch * rjz) * e;
+        const double w = X[i * n + j] * scale;
+        lx += w * gx;
+        ly += w * gy;
+        lz += w * gz;
+      } else {
+        double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
+        pbc(s, dx, dy, dz);
+        double g0, g1, g2;
+        const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
+        const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
+        const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
+        gx = g0 / (v0 + 1e-300);
+        gy = g1 / (v1v + 1e-300);
+        gz = g2 / (v2v + 1e-300);
+        gx *= v0; gy *= v0; gz *= v0;
+        gx *= v1v; gy *= v1v; gz *= v1v;
+        gx *= v2v; gy *= v2v; gz *= v2v;
+        const double w = X[i * n + j];
+        lx += w * gx * scale;
+        ly += w * gy * scale;
+        lz += w * gz * scale;
+      }
+    }
+    d1[j] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
+  }
+  if (lane < n) {
+    const int i = lane;  // d2: gradient with respect to r2_i
+    double rix, riy, riz;
+    v2.get(f + i, rix, riy, riz);
+    double lx = 0, ly = 0, lz = 0;
+    for (int j = 0; j < n; ++j) {
+      double rjx, rjy, rjz;
+      v1.get(f + j, rjx, rjy, rjz);
+      double gx, gy, gz;
+      if (sho) {
+        const double c = s.node_c[sp], ch = s.node_cosh[sp];
+        const double e = E[j * n + i];
+        gx = 2 * c * (rjx - ch * rix) * e;
+        gy = 2 * c * (rjy - ch * riy) * e;
+        gz = 2 * c * (rjz - ch * riz) * e;
+        const double w = X[i * n + j] * scale;
+        lx += w * gx;
+        ly += w * gy;
+        lz += w * gz;
+      } else {
+        double dx = rix - rjx, dy = riy - rjy, dz = riz - rjz;
+        pbc(s, dx, dy, dz);
+        double g0, g1, g2;
+        const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
+        const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
+        const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
+        gx = g0 / (v0 + 1e-300);
+        gy = g1 / (v1v + 1e-300);
+        gz = g2 / (v2v + 1e-300);
+        gx *= v0; gy *= v0; gz *= v0;
+        gx *= v1v; gy *= v1v; gz *= v1v;
+        gx *= v2v; gy *= v2v; gz *= v2v;
+        const double w = X[i * n + j];
+        lx += w * gx * scale;
+        ly += w * gy * scale;
+        lz += w * gz * scale;
+      }
+    }
+    d2[i] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------------ actions
+// Per-thread partial of CompositeAction::getActionDifference for one moving
+// particle ipart at one level: SpringAction (src/action/SpringAction.cc:56-98),
+// SHOAction (src/action/SHOAction.cc:19-65), PrimSHOAction
+// (src/action/PrimSHOAction.cc:21-58), PairAction per species pair
+// (src/action/PairAction.cc:219-360).  Work items are links and (partner, link)
+// pairs; each item contributes (new - old).
+__device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level) {
+  const int L = s.nlevel, np = s.npart;
+  const int nStride = 1 << level;
+  const int nlinks = 1 << (L - level);
+  const int sp = [&] {
+    int r = 0;
+    for (int k = 0; k < s.nspecies; ++k)
+      if (ipart >= s.spec_first[k] && ipart < s.spec_first[k] + s.spec_count[k]) r = k;
+    return r;
+  }();
+  double acc = 0.0;
+  // spring + SHO + PrimSHO: one item per link k (slices (k-1)*nStride, k*nStride)
+  const double lam = s.lambda[sp];
+  const double inv2Sigma2 = 0.25 / (lam * s.tau * nStride);
+  const double om = s.sho_omega[sp];
+  double coshwt = 0, div1 = 0, div2 = 0, msho = s.mass[sp];
+  if (om > 0) {
+    const double wt = om * s.tau * nStride;
+    coshwt = cosh(wt);
+    div1 = 1.0 / (2.0 * sinh(wt));
+    div2 = 1.0 / (2.0 * s.tau * nStride);
+  }
+  const bool prim = s.prim_a[sp] != 0 || s.prim_b[sp] != 0;
+  // Pair tables the moving particle takes part in, and their partner ranges.
+  int tb[kMaxTables], tjb[kMaxTables], tn[kMaxTables], nt = 0;
+  if (s.coulomb) {
+    for (int ti = 0; ti < s.ntab; ++ti) {
+      const DevTable& t = s.tab[ti];
+      if (ipart >= t.ifirst1 && ipart < t.ifirst1 + t.npart1) {
+        tb[nt] = ti;
+        tjb[nt] = t.ifirst2;
+        tn[nt++] = t.npart2;
+      } else if (ipart >= t.ifirst2 && ipart < t.ifirst2 + t.npart2) {
+        tb[nt] = ti;
+        tjb[nt] = t.ifirst1;
+        tn[nt++] = t.npart1;
+      }
+    }
+  }
+  int total = nlinks;
+  for (int q = 0; q < nt; ++q) total += tn[q] * nlinks;
+  for (int item = threadIdx.x; item < total; item += blockDim.x) {
+    if (item < nlinks) {
+      const int k = item + 1;
+      const int t1 = k * nStride, t0 = t1 - nStride;
+      const double n1x = m.mx[t1], n1y = m.my[t1], n1z = m.mz[t1];
+      const double n0x = m.mx[t0], n0y = m.my[t0], n0z = m.mz[t0];
+      const double o1x = m.s1x[t1 * np + ipart], o1y = m.s1y[t1 * np + ipart], o1z = m.s1z[t1 * np + ipart];
+      const double o0x = m.s1x[t0 * np + ipart], o0y = m.s1y[t0 * np + ipart], o0z = m.s1z[t0 * np + ipart];
+      if (s.spring) {
+        double dx = n1x - n0x, dy = n1y - n0y, dz = n1z - n0z;
+        pbc(s, dx, dy, dz);
+        double ex = o1x - o0x, ey = o1y - o0y, ez = o1z - o0z;
+        pbc(s, ex, ey, ez);
+        const double nw = dx * dx * inv2Sigma2 + dy * dy * inv2Sigma2 + dz * dz * inv2Sigma2;
+        const double od = ex * ex * inv2Sigma2 + ey * ey * inv2Sigma2 + ez * ez * inv2Sigma2;
+        acc += nw - od;
+      }
+      if (om > 0) {
+        double r0r0 = n0x * n0x + n0y * n0y + n0z * n0z;
+        double r1r1 = n1x * n1x + n1y * n1y + n1z * n1z;
+        double r0r1 = n0x * n1x + n0y * n1y + n0z * n1z;
+        double dx = n1x - n0x, dy = n1y - n0y, dz = n1z - n0z;
+        double d2 = dx * dx + dy * dy + dz * dz;
+        const double nw = msho * om * ((r1r1 + r0r0) * coshwt - 2.0 * r0r1) * div1 - msho * d2 * div2;
+        r0r0 = o0x * o0x + o0y * o0y + o0z * o0z;
+        r1r1 = o1x * o1x + o1y * o1y + o1z * o1z;
+        r0r1 = o0x * o1x + o0y * o1y + o0z * o1z;
+        dx = o1x - o0x;
+        dy = o1y - o0y;
+        dz = o1z - o0z;
+        d2 = dx * dx + dy * dy + dz * dz;
+        const double od = msho * om * ((r1r1 + r0r0) * coshwt - 2.0 * r0r1) * div1 - msho * d2 * div2;
+        acc += nw - od;
+      }
+      if (prim && k < nlinks) {
+        double x = n1x, y = n1y, z = n1z;
+        pbc(s, x, y, z);
+        double x2 = x * x + y * y + z * z;
+        const double kt = s.tau * nStride;
+        const double nw = (s.prim_a[sp] * x2 + s.prim_b[sp] * x2 * x2) * kt;
+        x = o1x;
+        y = o1y;
+        z = o1z;
+        pbc(s, x, y, z);
+        x2 = x * x + y * y + z * z;
+        acc += nw - (s.prim_a[sp] * x2 + s.prim_b[sp] * x2 * x2) * kt;
+      }
+      continue;
+    }
+    int it = item - nlinks, q = 0;
+    while (it >= tn[q] * nlinks) {
+      it -= tn[q] * nlinks;
+      ++q;
+    }
+    const DevTable& t = s.tab[tb[q]];
+    const int jj = it / nlinks;
+    const int j = tjb[q] + jj;
+    if (j == ipart) continue;
+    const int k = it - jj * nlinks + 1;
+    const int t1 = k * nStride, t0 = t1 - nStride;
+    const double pjx1 = m.s1x[t1 * np + j], pjy1 = m.s1y[t1 * np + j], pjz1 = m.s1z[t1 * np + j];
+    const double pjx0 = m.s1x[t0 * np + j], pjy0 = m.s1y[t0 * np + j], pjz0 = m.s1z[t0 * np + j];
+    const bool offdiag = level < 3 && t.norder > 0;
+    double act[2];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      double ax, ay, az, bx, by, bz;
+      if (pass == 0) {
+        ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
+        bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
+      } else {
+        ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
+        bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
+      }
+      double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
+      pbc(s, dx, dy, dz);
+      double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
+      pbc(s, px, py, pz);
+      const double r = sqrt(dot3(dx, dy, dz, dx, dy, dz));
+      const double rp = sqrt(dot3(px, py, pz, px, py, pz));
+      const double qq = 0.5 * (r + rp);
+      double a;
+      if (offdiag) {
+        const double sx = dx - px, sy = dy - py, sz = dz - pz;
+        const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (qq * qq);
+        a = tab_uk0(t, qq, s2) * nStride;
+      } else {
+        a = tab_u00(t, qq) * nStride;
+      }
+      act[pass] = a;
+    }
+    acc += act[0] - act[1];
+  }
+  return acc;
+}
+
+// EwaldSum::evalLongRange (src/util/EwaldSum.cc:103-181) for the old and the
+// new configuration of one slice (the new one has particle ipart at the moving
+// bead), as CoulombAction::getActionDifference uses them at level 0
+// (src/action/CoulombAction.cc:107-119).  Returns both evalLongRange values.
+__device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipart, int t, double& eold,
+                                 double& enew) {
+  const int np = s.npart;
+  const int kx0 = s.ikmax[0], ky0 = s.ikmax[1], kz0 = s.ikmax[2];
+  const int nx = kx0 + 1, ny = 2 * ky0 + 1, nz = 2 * kz0 + 1;
+  double2* X = (double2*)m.ewt;        // [nx][np+1], column np = moved bead
+  double2* Y = X + nx * (np + 1);      // [ny][np+1]
+  double2* Z = Y + ny * (np + 1);      // [nz][np+1]
+  const int w = np + 1;
+  __syncthreads();
+  for (int p = threadIdx.x; p < w; p += blockDim.x) {
+    double x, y, z;
+    if (p < np) {
+      x = m.s1x[t * np + p];
+      y = m.s1y[t * np + p];
+      z = m.s1z[t * np + p];
+    } else {
+      x = m.mx[t];
+      y = m.my[t];
+      z = m.mz[t];
+    }
+    X[p] = make_double2(1.0, 0.0);
+    Y[ky0 * w + p] = make_double2(1.0, 0.0);
+    Z[kz0 * w + p] = make_double2(1.0, 0.0);
+    double sn, cs;
+    if (kx0 > 0) {
+      sincos(s.deltak[0] * x, &sn, &cs);
+      X[w + p] = make_double2(cs, sn);
+    }
+    if (ky0 > 0) {
+      sincos(s.deltak[1] * y, &sn, &cs);
+      Y[(ky0 + 1) * w + p] = make_double2(cs, sn);
+      Y[(ky0 - 1) * w + p] = make_double2(cs, -sn);
+    }
+    if (kz0 > 0) {
+      sincos(s.deltak[2] * z, &sn, &cs);
+      Z[(kz0 + 1) * w + p] = make_double2(cs, sn);
+      Z[(kz0 - 1) * w + p] = make_double2(cs, -sn);
+    }
+    const double2 x1 = X[w + p];
+    for (int k = 2; k <= kx0; ++k) {
+      const double2 a = X[(k - 1) * w + p];
+      X[k * w + p] = make_double2(a.x * x1.x - a.y * x1.y, a.x * x1.y + a.y * x1.x);
+    }
+    const double2 yp = Y[(ky0 + 1) * w + p], ym = Y[(ky0 - 1) * w + p];
+    for (int k = 2; k <= ky0; ++k) {
+      double2 a = Y[(ky0 + k - 1) * w + p];
+      Y[(ky0 + k) * w + p] = make_double2(a.x * yp.x - a.y * yp.y, a.x * yp.y + a.y * yp.x);
+      a = Y[(ky0 - k + 1) * w + p];
+      Y[(ky0 - k) * w + p] = make_double2(a.x * ym.x - a.y * ym.y, a.x * ym.y + a.y * ym.x);
+    }
+    const double2 zp = Z[(kz0 + 1) * w + p], zm = Z[(kz0 - 1) * w + p];
+    for (int k = 2; k <= kz0; ++k) {
+      double2 a = Z[(kz0 + k - 1) * w + p];
+      Z[(kz0 + k) * w + p] = make_double2(a.x * zp.x - a.y * zp.y, a.x * zp.y + a.y * zp.x);
+      a = Z[(kz0 - k + 1) * w + p];
+      Z[(kz0 - k) * w + p] = make_double2(a.x * zm.x - a.y * zm.y, a.x * zm.y + a.y * zm.x);
+    }
+  }
+  __syncthreads();
+  double so = 0.0, sn_ = 0.0;
+  for (int k = threadIdx.x; k < s.totk; k += blockDim.x) {
+    const int kx = __ldg(s.kvec + 3 * k), ky = __ldg(s.kvec + 3 * k + 1) + ky0,
+              kz = __ldg(s.kvec + 3 * k + 2) + kz0;
+    double cor = 0, coi = 0, cnr = 0, cni = 0;
+    for (int j = 0; j < np; ++j) {
+      const int jj = (j == ipart) ? np : j;
+      const double qj = m.qpart[j];
+      double2 a = X[kx * w + j];
+      double tr = qj * a.x, ti = qj * a.y;
+      double2 b = Y[ky * w + j];
+      double ur = tr * b.x - ti * b.y, ui = tr * b.y + ti * b.x;
+      b = Z[kz * w + j];
+      const double vr = ur * b.x - ui * b.y, vi = ur * b.y + ui * b.x;
+      cor += vr;
+      coi += vi;
+      if (jj == j) {
+        cnr += vr;
+        cni += vi;
+      } else {
+        a = X[kx * w + jj];
+        tr = qj * a.x;
+        ti = qj * a.y;
+        b = Y[ky * w + jj];
+        ur = tr * b.x - ti * b.y;
+        ui = tr * b.y + ti * b.x;
+        b = Z[kz * w + jj];
+        cnr += ur * b.x - ui * b.y;
+        cni += ur * b.y + ui * b.x;
+      }
+    }
+    const double vk = __ldg(s.vk + k);
+    so += 2 * vk * (cor * cor + coi * coi);
+    sn_ += 2 * vk * (cnr * cnr + cni * cni);
+  }
+  const double old_sum = block_sum(so, m.red);
+  const double new_sum = block_sum(sn_, m.red);
+  eold = old_sum * s.one_over_2v + s.self_energy;
+  enew = new_sum * s.one_over_2v + s.self_energy;
+}
+
+// (new - old) * tau / epsilon of one slice, the level-0 Ewald term.
+__device__ double ewald_slice_diff(const DevSys& s, const Smem& m, int ipart, int t) {
+  double eold, enew;
+  ewald_slice_sums(s, m, ipart, t, eold, enew);
+  return -(eold * s.tau / s.epsilon) + enew * s.tau / s.epsilon;
+}
+
+// evalLongRange of section slice t as staged in shared memory.
+__device__ double ewald_slice_energy(const DevSys& s, const Smem& m, int t) {
+  double eold, enew;
+  ewald_slice_sums(s, m, -1, t, eold, enew);
+  return eold;
+}
+
+}  // namespace pimc

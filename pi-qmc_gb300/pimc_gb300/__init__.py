@@ -1,0 +1,368 @@
+"""pimc_gb300 — Python host binding of the GB300 PIMC engine's C ABI.
+
+The engine (libpimc_gb300.so, built by ``pimc_gb300.build``) runs pi-qmc's
+multilevel-bisection hot path on an sm_103a GPU.  This module is a thin ctypes
+layer over include/pimc_gb300.h; names follow pi-qmc (SimulationInfo fields,
+getActionDifference, NodeModel::evaluate, ThermoEnergyEstimator).  There is no
+CPU fallback: without the library or a GPU every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+MAXS = 4
+MAXL = 6
+PIMC_NODES_NONE, PIMC_NODES_SHO, PIMC_NODES_FREE = 0, 1, 2
+PIMC_MOVER_FREE, PIMC_MOVER_FREE_PBC = 0, 1
+PIMC_PREC_FP64, PIMC_PREC_MIXED = 0, 1
+STATUS_BITS = {1: "init_crossing", 2: "singular", 4: "rescale_limit", 8: "nonfinite"}
+
+
+class PimcError(RuntimeError):
+    pass
+
+
+class System(C.Structure):
+    """pimc_system: one simulated system (SimulationInfo + action attributes)."""
+    _fields_ = [
+        ("npart", C.c_int), ("nspecies", C.c_int),
+        ("spec_count", C.c_int * MAXS), ("spec_mass", C.c_double * MAXS),
+        ("spec_charge", C.c_double * MAXS), ("sho_omega", C.c_double * MAXS),
+        ("prim_a", C.c_double * MAXS), ("prim_b", C.c_double * MAXS),
+        ("node_kind", C.c_int * MAXS), ("node_omega", C.c_double * MAXS),
+        ("node_temperature", C.c_double), ("nslice", C.c_int), ("tau", C.c_double),
+        ("nlevel", C.c_int), ("cell", C.c_double * 3), ("spring", C.c_int),
+        ("coulomb", C.c_int), ("epsilon", C.c_double), ("ewald", C.c_int), ("mover", C.c_int),
+    ]
+
+
+class PairTable(C.Structure):
+    _fields_ = [("species1", C.c_int), ("species2", C.c_int), ("ngpts", C.c_int),
+                ("norder", C.c_int), ("rgridinv", C.c_double), ("logrratioinv", C.c_double),
+                ("ugrid", C.POINTER(C.c_double))]
+
+
+class EwaldTable(C.Structure):
+    _fields_ = [("totk", C.c_int), ("kvec", C.POINTER(C.c_int)), ("vk", C.POINTER(C.c_double)),
+                ("one_over_2v", C.c_double), ("self_energy", C.c_double), ("ikmax", C.c_int * 3)]
+
+
+class MoveRecord(C.Structure):
+    _fields_ = [("ifirst1", C.c_int), ("ifirst2", C.c_int), ("ipart", C.c_int),
+                ("reject_level", C.c_int), ("ds", C.c_double * (MAXL + 3)),
+                ("ds_node", C.c_double * (MAXL + 3)), ("lnt", C.c_double * (MAXL + 3))]
+
+
+def system_from_kw(kw):
+    """A pimc_system from workload keywords (see pimc_gb300.workloads)."""
+    s = System()
+    counts = kw["counts"]
+    ns = len(counts)
+    s.nspecies = ns
+    s.npart = int(sum(counts))
+    get = lambda k, d: kw.get(k, [d] * ns)  # noqa: E731
+    for i in range(ns):
+        s.spec_count[i] = counts[i]
+        s.spec_mass[i] = get("masses", 1.0)[i]
+        s.spec_charge[i] = get("charges", -1.0)[i]
+        s.sho_omega[i] = get("sho_omega", 0.0)[i]
+        s.prim_a[i] = get("prim_a", 0.0)[i]
+        s.prim_b[i] = get("prim_b", 0.0)[i]
+        s.node_kind[i] = get("node_kind", 0)[i]
+        s.node_omega[i] = get("node_omega", 0.0)[i]
+    s.nslice = kw["nslice"]
+    s.tau = kw["beta"] / kw["nslice"]
+    s.node_temperature = kw.get("node_temperature", 1.0 / kw["beta"])
+    s.nlevel = kw["nlevel"]
+    cell = kw.get("cell", 1000.0)
+    cell = cell if hasattr(cell, "__len__") else [cell] * 3
+    for d in range(3):
+        s.cell[d] = cell[d]
+    s.spring = kw.get("spring", 1)
+    s.coulomb = kw.get("coulomb", 0)
+    s.epsilon = kw.get("epsilon", 1.0)
+    s.ewald = kw.get("ewald", 0)
+    s.mover = kw.get("mover", 0)
+    return s
+
+
+_lib = None
+
+
+def lib():
+    """Load the engine library (fails loudly if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise PimcError(f"engine library not built: {LIB_PATH} (run pimc_gb300.build)")
+        L = C.CDLL(LIB_PATH)
+        P, I, D = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+        L.pimc_last_error.restype = C.c_char_p
+        L.pimc_engine_create.argtypes = [C.POINTER(System), I, C.POINTER(PairTable), I,
+                                         C.POINTER(EwaldTable), C.c_uint64, I, C.POINTER(P)]
+        L.pimc_engine_create_batch.argtypes = [C.POINTER(System), I, C.POINTER(PairTable),
+                                               C.POINTER(C.c_int), C.c_uint64, I, C.POINTER(P)]
+        L.pimc_engine_destroy.argtypes = [P]
+        L.pimc_set_stream.argtypes = [P, P]
+        L.pimc_upload_paths.argtypes = [P, D]
+        L.pimc_download_paths.argtypes = [P, D]
+        L.pimc_path_offsets.argtypes = [P, C.POINTER(C.c_int64)]
+        L.pimc_run_sections.argtypes = [P, I, C.POINTER(MoveRecord)]
+        L.pimc_replica_status.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_uint32)]
+        L.pimc_thermo_energy.argtypes = [P, D]
+        L.pimc_action_difference.argtypes = [P, I, I, D, D, C.POINTER(C.c_int), D]
+        L.pimc_node_evaluate.argtypes = [P, I, I, D, D, D, D, D, C.POINTER(C.c_int)]
+        L.pimc_node_scale.argtypes = [P, I, I, D]
+        L.pimc_stream_sample.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, I, D, D]
+        L.pimc_kernel_launches.argtypes = [P]
+        L.pimc_kernel_launches.restype = C.c_int64
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise PimcError(f"pimc error {rc}: {lib().pimc_last_error().decode()}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def pair_tables_struct(tables):
+    """Array of PairTable from dicts with species/ngpts/norder/rgridinv/logrratioinv/ugrid."""
+    n = len(tables)
+    arr = (PairTable * max(n, 1))()
+    keep = []
+    for k, t in enumerate(tables):
+        ug = np.ascontiguousarray(t["ugrid"], np.float64)
+        keep.append(ug)
+        s1, s2 = t["species"]
+        arr[k].species1, arr[k].species2 = int(s1), int(s2)
+        arr[k].ngpts, arr[k].norder = int(t["ngpts"]), int(t["norder"])
+        arr[k].rgridinv, arr[k].logrratioinv = float(t["rgridinv"]), float(t["logrratioinv"])
+        arr[k].ugrid = _dp(ug)
+    return arr, keep
+
+
+def ewald_struct(ew):
+    if ew is None:
+        return None, []
+    kv = np.ascontiguousarray(ew["kvec"], np.int32)
+    vk = np.ascontiguousarray(ew["vk"], np.float64)
+    e = EwaldTable()
+    e.totk = int(ew["totk"])
+    e.kvec = kv.ctypes.data_as(C.POINTER(C.c_int))
+    e.vk = _dp(vk)
+    e.one_over_2v = float(ew["one_over_2v"])
+    e.self_energy = float(ew["self_energy"])
+    for d in range(3):
+        e.ikmax[d] = int(ew["ikmax"][d])
+    return e, [kv, vk]
+
+
+def records_to_numpy(recs, n):
+    out = {
+        "ifirst1": np.array([r.ifirst1 for r in recs[:n]], np.int32),
+        "ifirst2": np.array([r.ifirst2 for r in recs[:n]], np.int32),
+        "ipart": np.array([r.ipart for r in recs[:n]], np.int32),
+        "reject_level": np.array([r.reject_level for r in recs[:n]], np.int32),
+        "ds": np.array([list(r.ds) for r in recs[:n]]),
+        "ds_node": np.array([list(r.ds_node) for r in recs[:n]]),
+        "lnt": np.array([list(r.lnt) for r in recs[:n]]),
+    }
+    return out
+
+
+def stream_sample(seed, replica, attempt, n):
+    """The first n uniforms and normals of one attempt's streams, generated on
+    the GPU (for bit-exact comparison with a CPU replay)."""
+    u = np.zeros(n)
+    z = np.zeros(n)
+    _check(lib().pimc_stream_sample(C.c_uint64(seed), replica, attempt, n, _dp(u), _dp(z)))
+    return u, z
+
+
+class Engine:
+    """A set of replicas advanced on the GPU (pimc_engine).
+
+    ``Engine(system_kw, nreplica, tables, ewald, seed)`` builds replicas of one
+    system; ``Engine.batch([kw...], [tables...], seed)`` builds uneven replicas.
+    """
+
+    def __init__(self, system_kw=None, nreplica=1, tables=(), ewald=None, seed=20261203,
+                 precision=PIMC_PREC_FP64, _handle=None, _systems=None):
+        L = lib()
+        self.precision = precision
+        if _handle is not None:
+            self.h = _handle
+            self.systems = _systems
+        else:
+            sysc = system_from_kw(system_kw)
+            tabs, self._keep = pair_tables_struct(tables)
+            ew, keep2 = ewald_struct(ewald)
+            self._keep += keep2
+            h = C.c_void_p()
+            _check(L.pimc_engine_create(C.byref(sysc), nreplica, tabs, len(tables),
+                                        C.byref(ew) if ew is not None else None,
+                                        C.c_uint64(seed), precision, C.byref(h)))
+            self.h = h
+            self.systems = [sysc] * nreplica
+        self.nreplica = len(self.systems)
+        offs = (C.c_int64 * (self.nreplica + 1))()
+        _check(L.pimc_path_offsets(self.h, offs))
+        self.offsets = np.array(list(offs), np.int64)
+
+    @classmethod
+    def batch(cls, system_kws, tables_per_replica, seed=20261203, precision=PIMC_PREC_FP64):
+        L = lib()
+        n = len(system_kws)
+        systems = (System * n)(*[system_from_kw(kw) for kw in system_kws])
+        flat = [t for ts in tables_per_replica for t in ts]
+        tabs, keep = pair_tables_struct(flat)
+        off = np.zeros(n + 1, np.int32)
+        off[1:] = np.cumsum([len(ts) for ts in tables_per_replica])
+        h = C.c_void_p()
+        _check(L.pimc_engine_create_batch(systems, n, tabs,
+                                          off.ctypes.data_as(C.POINTER(C.c_int)),
+                                          C.c_uint64(seed), precision, C.byref(h)))
+        e = cls(_handle=h, _systems=list(systems), precision=precision)
+        e._keep = keep
+        return e
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pimc_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib().pimc_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    # paths ----------------------------------------------------------------
+    def path_shape(self, r):
+        s = self.systems[r]
+        return (s.nslice, s.npart, 3)
+
+    def upload_paths(self, paths):
+        """paths: one array [nslice][npart][3] per replica, or a packed flat array."""
+        if isinstance(paths, np.ndarray) and paths.ndim == 1:
+            flat = np.ascontiguousarray(paths, np.float64)
+        else:
+            flat = np.concatenate([np.ascontiguousarray(p, np.float64).ravel() for p in paths])
+        assert flat.size == self.offsets[-1]
+        _check(lib().pimc_upload_paths(self.h, _dp(flat)))
+        self._last_upload = flat
+
+    def download_paths(self, flat=False):
+        out = np.empty(int(self.offsets[-1]))
+        _check(lib().pimc_download_paths(self.h, _dp(out)))
+        if flat:
+            return out
+        return [out[self.offsets[r]:self.offsets[r + 1]].reshape(self.path_shape(r))
+                for r in range(self.nreplica)]
+
+    # sampler --------------------------------------------------------------
+    def run_sections(self, nattempt, records=False):
+        """nattempt section-move attempts on every replica (asynchronous unless
+        records are requested)."""
+        if records:
+            recs = (MoveRecord * (self.nreplica * nattempt))()
+            _check(lib().pimc_run_sections(self.h, nattempt, recs))
+            r = records_to_numpy(recs, self.nreplica * nattempt)
+            return {k: v.reshape((self.nreplica, nattempt) + v.shape[1:]) for k, v in r.items()}
+        _check(lib().pimc_run_sections(self.h, nattempt, None))
+        return None
+
+    def replica_status(self):
+        n = self.nreplica
+        acc = np.zeros(n, np.int64)
+        att = np.zeros(n, np.int64)
+        st = np.zeros(n, np.uint32)
+        _check(lib().pimc_replica_status(self.h, acc.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         att.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         st.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return acc, att, st
+
+    def node_scale(self, replica, ispec):
+        v = C.c_double()
+        _check(lib().pimc_node_scale(self.h, replica, ispec, C.byref(v)))
+        return v.value
+
+    # estimators -----------------------------------------------------------
+    def thermo_energy(self):
+        out = np.zeros(self.nreplica)
+        _check(lib().pimc_thermo_energy(self.h, _dp(out)))
+        return out
+
+    # Action / NodeModel level ---------------------------------------------
+    def action_difference(self, level, sections, movings, iparts):
+        sections = np.ascontiguousarray(sections, np.float64)
+        movings = np.ascontiguousarray(movings, np.float64)
+        ip = np.ascontiguousarray(iparts, np.int32)
+        nb = len(ip)
+        ds = np.zeros(nb)
+        _check(lib().pimc_action_difference(self.h, level, nb, _dp(sections), _dp(movings),
+                                            ip.ctypes.data_as(C.POINTER(C.c_int)), _dp(ds)))
+        return ds
+
+    def node_evaluate(self, ispec, r1, r2):
+        r1 = np.ascontiguousarray(r1, np.float64)
+        r2 = np.ascontiguousarray(r2, np.float64)
+        nb, np_ = r1.shape[0], r1.shape[1]
+        det = np.zeros(nb)
+        d1 = np.zeros((nb, np_))
+        d2 = np.zeros((nb, np_))
+        err = np.zeros(nb, np.int32)
+        _check(lib().pimc_node_evaluate(self.h, ispec, nb, _dp(r1), _dp(r2), _dp(det), _dp(d1),
+                                        _dp(d2), err.ctypes.data_as(C.POINTER(C.c_int))))
+        return err, det, d1, d2
+
+    @property
+    def kernel_launches(self):
+        return lib().pimc_kernel_launches(self.h)
+
+
+def coulomb_tables(system_kw, norder=3, ngpts=0, rmin=0.0, rmax=0.0, ewald_rcut=0.0):
+    """CoulombAction pair tables (and the OptEwaldSum table when the system has
+    Ewald) built by the engine's own host code; returns (tables, ewald) in the
+    form Engine() takes."""
+    L = lib()
+    if not hasattr(L, "_tables_bound"):
+        L.pimc_coulomb_tables.argtypes = [C.POINTER(System), C.c_int, C.c_int, C.c_double,
+                                          C.c_double, C.c_double, C.c_double,
+                                          C.POINTER(C.POINTER(PairTable)), C.POINTER(C.c_int),
+                                          C.POINTER(C.POINTER(EwaldTable))]
+        L._tables_bound = True
+    s = system_from_kw(system_kw)
+    tp = C.POINTER(PairTable)()
+    nt = C.c_int()
+    ep = C.POINTER(EwaldTable)()
+    _check(L.pimc_coulomb_tables(C.byref(s), norder, ngpts, rmin, rmax, ewald_rcut,
+                                 float(system_kw.get("ewald_kcut", 0.0)), C.byref(tp),
+                                 C.byref(nt), C.byref(ep)))
+    tables = []
+    for k in range(nt.value):
+        t = tp[k]
+        nd = t.norder + 1
+        ug = np.ctypeslib.as_array(t.ugrid, shape=(t.ngpts * 2 * nd,)).reshape(t.ngpts, 2, nd).copy()
+        tables.append(dict(species=(t.species1, t.species2), ngpts=t.ngpts, norder=t.norder,
+                           rgridinv=t.rgridinv, logrratioinv=t.logrratioinv, ugrid=ug))
+    ewald = None
+    if ep:
+        e = ep.contents
+        ewald = dict(totk=e.totk,
+                     kvec=np.ctypeslib.as_array(e.kvec, shape=(e.totk * 3,)).reshape(-1, 3).copy(),
+                     vk=np.ctypeslib.as_array(e.vk, shape=(e.totk,)).copy(),
+                     one_over_2v=e.one_over_2v, self_energy=e.self_energy, ikmax=list(e.ikmax))
+    return tables, ewald

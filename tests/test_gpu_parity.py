@@ -1,0 +1,160 @@
+"""Parity of the CUDA engine with the CPU checkers, through the C ABI.
+
+Inputs are the golden fixtures made by pi-qmc's own code (tests/golden) and
+seeded synthetic sections; the checker is the C++ restatement (oracle/port.cc),
+itself pinned to the reference by tests/test_oracle.py.
+
+Tolerances: plain action differences and mover ratios 1e-12 relative (to
+max(|value|, 1)); section-move decisions (section start, particle, rejecting
+level) exact; paths 1e-12; node-model terms 1e-10 relative, except the
+omega/T = 20 SHO dot whose Slater matrices have condition numbers ~1e9 (see
+tests/test_oracle.py), held to 1e-2 relative on the nodal action with exact
+decisions.
+"""
+import numpy as np
+import pytest
+
+import golden_io
+import oracle_lib as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+NODE_TOL = {"dot20_fn": 1e-2}
+
+
+def rel_close(a, b, tol, floor=1.0):
+    return np.all(np.abs(a - b) <= tol * np.maximum(np.abs(a), floor))
+
+
+@pytest.fixture(scope="module")
+def pimc():
+    import pimc_gb300
+    pimc_gb300.build.build()
+    return pimc_gb300
+
+
+def engine_for(pimc, g, nreplica=1, seed=20261203):
+    return pimc.Engine(g["kw"], nreplica, g["tables"], g["ewald"], seed=seed)
+
+
+def test_streams_bit_exact(pimc):
+    # The engine's uniforms and normals equal the CPU replay bit for bit.
+    for rep, att in [(0, 0), (3, 17), (4095, 123456)]:
+        u, z = pimc.stream_sample(20261203, rep, att, 256)
+        cu, cz = O.cpu_stream(20261203, rep, att, 256)
+        assert np.array_equal(u, cu)
+        assert np.array_equal(z, cz)
+
+
+@pytest.mark.parametrize("case", list(W.GOLDEN_CASES))
+def test_sampler_matches_golden(pimc, case):
+    g = golden_io.load(case)
+    e = engine_for(pimc, g)
+    e.upload_paths([g["path0"]])
+    rec = e.run_sections(g["nattempt"], records=True)
+    ref = g["records"]
+    for k in ("ifirst1", "ifirst2", "ipart", "reject_level"):
+        assert np.array_equal(rec[k][0], ref[k]), k
+    nl = g["kw"]["nlevel"] + 1
+    assert rel_close(rec["ds"][0][:, :nl], ref["ds"][:, :nl], 1e-12)
+    assert rel_close(rec["lnt"][0][:, :nl], ref["lnt"][:, :nl], 1e-12)
+    assert rel_close(rec["ds_node"][0][:, :nl], ref["ds_node"][:, :nl],
+                     NODE_TOL.get(case, 1e-10))
+    path = e.download_paths()[0]
+    assert np.abs(path - g["path1"]).max() <= 1e-12
+    acc, att, st = e.replica_status()
+    assert acc[0] == g["naccepted"] and att[0] == g["nattempt"]
+    assert e.thermo_energy()[0] == pytest.approx(g["energy1"], rel=1e-12)
+
+
+def test_replicas_follow_their_own_streams(pimc):
+    # Replica r of an engine reproduces the checker run with replica id r.
+    g = golden_io.load("dot2_small")
+    R = 5
+    e = engine_for(pimc, g, nreplica=R, seed=777)
+    paths = [W.initial_path(O.make_config(**g["kw"]), "gauss", seed=100 + r) for r in range(R)]
+    e.upload_paths(paths)
+    rec = e.run_sections(200, records=True)
+    out = e.download_paths()
+    for r in range(R):
+        cfg = O.make_config(**dict(g["kw"], seed=777, replica=r))
+        port = O.PortOracle(cfg, g["tables"], g["ewald"])
+        port.set_path(paths[r])
+        pr = port.run(200)
+        assert np.array_equal(pr["reject_level"], rec["reject_level"][r])
+        assert np.array_equal(pr["ipart"], rec["ipart"][r])
+        assert rel_close(pr["ds"], rec["ds"][r][:, :9], 1e-12)
+        assert np.abs(port.get_path() - out[r]).max() <= 1e-12
+
+
+def test_second_launch_continues_the_chain(pimc):
+    # Two launches of n attempts equal one launch of 2n (attempt counters persist).
+    g = golden_io.load("dot2_small")
+    a = engine_for(pimc, g)
+    b = engine_for(pimc, g)
+    a.upload_paths([g["path0"]])
+    b.upload_paths([g["path0"]])
+    a.run_sections(300)
+    a.run_sections(300)
+    b.run_sections(600)
+    assert np.array_equal(a.download_paths()[0], b.download_paths()[0])
+
+
+@pytest.mark.parametrize("case", ["dot2_small", "heg8"])
+def test_action_difference_every_level(pimc, case):
+    g = golden_io.load(case)
+    cfg = O.make_config(**g["kw"])
+    port = O.PortOracle(cfg, g["tables"], g["ewald"])
+    e = engine_for(pimc, g)
+    rng = np.random.default_rng(3)
+    nsec = (1 << cfg.nlevel) + 1
+    nb = 24
+    secs = g["path0"][:nsec][None].repeat(nb, 0) + 0.05 * rng.normal(size=(nb, nsec, cfg.npart, 3))
+    ips = rng.integers(0, cfg.npart, nb)
+    movs = np.stack([secs[b, :, ips[b], :] for b in range(nb)])
+    movs[:, 1:-1] += 0.2 * rng.normal(size=(nb, nsec - 2, 3))
+    for level in range(cfg.nlevel + 1):
+        ds = e.action_difference(level, secs, movs, ips)
+        for b in range(nb):
+            ref = port.action_diff(level, secs[b], movs[b], int(ips[b]))
+            assert abs(ds[b] - ref) <= 1e-12 * max(abs(ref), 1.0), (level, b)
+
+
+@pytest.mark.parametrize("case", ["dot4_fn", "heg8"])
+def test_node_evaluate(pimc, case):
+    g = golden_io.load(case)
+    cfg = O.make_config(**g["kw"])
+    port = O.PortOracle(cfg, g["tables"], g["ewald"])
+    e = engine_for(pimc, g)
+    rng = np.random.default_rng(9)
+    nb = 16
+    base = g["path0"][0]
+    r1 = base[None] + 0.3 * rng.normal(size=(nb, cfg.npart, 3))
+    r2 = base[None] + 0.3 * rng.normal(size=(nb, cfg.npart, 3))
+    for sp in range(cfg.nspecies):
+        err, det, d1, d2 = e.node_evaluate(sp, r1, r2)
+        for b in range(nb):
+            perr, pdet, pd1, pd2 = port.node_eval(sp, r1[b], r2[b], 0, False)
+            assert err[b] == perr
+            assert abs(det[b] - pdet) <= 1e-10 * abs(pdet)
+            assert rel_close(d1[b], pd1, 1e-10)
+            assert rel_close(d2[b], pd2, 1e-10)
+
+
+def test_thermo_energy_matches_checker(pimc):
+    for case in ("dot2_full", "heg8"):
+        g = golden_io.load(case)
+        e = engine_for(pimc, g)
+        e.upload_paths([g["path1"]])
+        assert e.thermo_energy()[0] == pytest.approx(g["energy1"], rel=1e-12)
+
+
+def test_kernel_launch_count(pimc):
+    g = golden_io.load("dot2_small")
+    e = engine_for(pimc, g)
+    e.upload_paths([g["path0"]])
+    n0 = e.kernel_launches
+    e.run_sections(10)
+    e.run_sections(10)
+    assert e.kernel_launches - n0 == 2

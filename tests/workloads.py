@@ -13,6 +13,6 @@ GOLDEN_CASES = {
     "dot2_full": (dot2(), "gauss", 400),
     "dot4_fn": (dot20_fn(counts=[2, 2], nslice=64, beta=4.0, nlevel=3), "const", 400),
     "dot20_fn": (dot20_fn(), "const", 40),
-    "heg8": (heg54(n=8, nslice=32, nlevel=3), "grid", 150),
+    "heg8": (heg54(n=8, nslice=128, nlevel=3), "grid", 150),
     "heg54": (heg54(), "grid", 12),
 }
