@@ -639,6 +639,34 @@ int pimc_stream_sample(uint64_t seed, uint32_t replica, uint32_t attempt, int n,
   return PIMC_OK;
 }
 
+int pimc_fp64_peak(double* tflops) {
+  if (!tflops) return fail(PIMC_ERR_INVALID, "null argument");
+  int nsm = 0;
+  if (int rc = device_check(nsm)) return rc;
+  double* d = nullptr;
+  CU(cudaMalloc(&d, sizeof(double)));
+  const int iters = 4096, blocks = nsm * 8, threads = 256;
+  fp64_probe_kernel<<<blocks, threads>>>(d, 16);
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    CU(cudaEventRecord(a));
+    fp64_probe_kernel<<<blocks, threads>>>(d, iters);
+    CU(cudaEventRecord(b));
+    CU(cudaEventSynchronize(b));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return PIMC_OK;
+}
+
 int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
 
 }  // extern "C"

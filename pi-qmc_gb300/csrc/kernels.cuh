@@ -712,6 +712,18 @@ __global__ void __launch_bounds__(kBlock) node_eval_kernel(NodeEvalParams P) {
   }
 }
 
+// FP64 FMA throughput probe: each thread runs independent FMA chains.
+__global__ void fp64_probe_kernel(double* out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double b = 0.999999999, c = 1e-12;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5) out[0] = a0;
+}
+
 __global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, int n, double* u,
                                      double* z) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -119,6 +119,7 @@ def lib():
         L.pimc_node_evaluate.argtypes = [P, I, I, D, D, D, D, D, C.POINTER(C.c_int)]
         L.pimc_node_scale.argtypes = [P, I, I, D]
         L.pimc_stream_sample.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, I, D, D]
+        L.pimc_fp64_peak.argtypes = [D]
         L.pimc_kernel_launches.argtypes = [P]
         L.pimc_kernel_launches.restype = C.c_int64
         _lib = L
@@ -177,6 +178,13 @@ def records_to_numpy(recs, n):
         "lnt": np.array([list(r.lnt) for r in recs[:n]]),
     }
     return out
+
+
+def fp64_peak_tflops():
+    """Measured dense FP64 FMA throughput of the device (TFLOP/s)."""
+    v = C.c_double()
+    _check(lib().pimc_fp64_peak(C.byref(v)))
+    return v.value
 
 
 def stream_sample(seed, replica, attempt, n):
