@@ -69,6 +69,7 @@ struct pimc_engine {
   DevBuf<int> d_kvec;
   DevBuf<double> d_vk;
   Layout lay{};
+  int block = kBlock;
   int grid = 0;
   int num_sms = 0;
   long long launches = 0;
@@ -168,6 +169,31 @@ void fill_sys(const pimc_system& s, DevSys& d) {
     }
   }
   d.tau = s.tau;
+  for (int lev = 0; lev < kMaxLevels; ++lev) {
+    const int nStride = 1 << lev;
+    d.sho_div2[lev] = 1.0 / (2.0 * s.tau * nStride);
+    for (int i = 0; i < s.nspecies; ++i) {
+      const double lam = 0.5 / s.spec_mass[i];
+      d.spr_inv2s2[lev][i] = 0.25 / (lam * s.tau * nStride);
+      const double sigma = 1.0 * std::sqrt(lam * s.tau * nStride);
+      d.mov_sigma[lev][i] = sigma;
+      d.mov_inv2s2[lev][i] = 0.5 / (sigma * sigma);
+      if (s.sho_omega[i] > 0) {
+        const double wt = s.sho_omega[i] * s.tau * nStride;
+        d.sho_cosh[lev][i] = std::cosh(wt);
+        d.sho_div1[lev][i] = 1.0 / (2.0 * std::sinh(wt));
+      }
+    }
+  }
+  for (int i = 0; i < s.nspecies; ++i) {
+    if (s.sho_omega[i] > 0) {
+      const double wt = s.sho_omega[i] * s.tau;
+      const double sinhwt = std::sinh(wt), coshwt = std::cosh(wt);
+      d.sho_cosh0[i] = coshwt;
+      d.sho_csch[i] = 1.0 / sinhwt;
+      d.sho_coth[i] = coshwt * d.sho_csch[i];
+    }
+  }
   for (int a = 0; a < 3; ++a) {
     d.cell[a] = s.cell[a];
     d.cellb[a] = 1. / s.cell[a];
@@ -186,7 +212,7 @@ void fill_sys(const pimc_system& s, DevSys& d) {
   d.epsilon = s.epsilon > 0 ? s.epsilon : 1.0;
 }
 
-Layout make_layout(const std::vector<DevSys>& sys, bool& ok) {
+Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
   int nsec = 0, np = 0, nsm = 1, ewt = 0;
   bool fixed = false;
   for (const DevSys& d : sys) {
@@ -216,10 +242,10 @@ Layout make_layout(const std::vector<DevSys>& sys, bool& ok) {
   L.ewt = take(ewt);
   L.ictl = take((C_NCTL + nsec + 1) / 2 + 1);
   L.nodescr_stride = fixed ? ((3 * nsm * nsm + 1) & ~1) : 0;
-  const int need = off + kWarps * L.nodescr_stride;
+  const int need = off + nwarps * L.nodescr_stride;
   const int limit = 200 * 1024 / 8;
   if (need <= limit) {
-    L.nodescr = take(kWarps * L.nodescr_stride);
+    L.nodescr = take(nwarps * L.nodescr_stride);
     L.nodescr_in_smem = 1;
   } else {
     L.nodescr = -1;
@@ -330,8 +356,21 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
     off += 3LL * s.nslice * s.npart;
   }
   e->path_off[nrep] = off;
+  // Block size: the widest level-0 work list decides.  Small systems without
+  // node models run one or two warps per replica so that replicas pack densely.
+  {
+    int items = 0;
+    bool fixed = false;
+    for (const DevSys& d : e->hsys) {
+      const int links = 1 << d.nlevel;
+      items = std::max(items, links * std::max(1, d.npart));
+      fixed |= d.fixed_node != 0;
+    }
+    e->block = fixed ? kBlock : (items <= 64 ? 64 : (items <= 128 ? 128 : kBlock));
+  }
+  for (DevSys& d : e->hsys) d.mixed = precision == PIMC_PREC_MIXED;
   bool ok = false;
-  e->lay = make_layout(e->hsys, ok);
+  e->lay = make_layout(e->hsys, e->block / 32, ok);
   if (!ok) {
     delete e;
     return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
@@ -372,13 +411,13 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        e->lay.total * 8);
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, kBlock,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, e->block,
                                                 e->lay.total * 8);
   occ = std::max(occ, 1);
   e->grid = std::min(nrep, nsm * occ);
   if (!e->lay.nodescr_in_smem) {
     for (DevSys& d : e->hsys) d.inv_offset = 0;
-    if (e->d_nodescr.alloc((size_t)e->grid * kWarps * e->lay.nodescr_stride)) {
+    if (e->d_nodescr.alloc((size_t)e->grid * (e->block / 32) * e->lay.nodescr_stride)) {
       delete e;
       return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
     }
@@ -475,7 +514,7 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
   P.nrep = e->nrep;
   P.seed = e->seed;
   P.lay = e->lay;
-  section_moves_kernel<<<e->grid, kBlock, e->lay.total * 8, e->stream>>>(P);
+  section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
   if (records) {

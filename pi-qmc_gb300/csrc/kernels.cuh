@@ -52,7 +52,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.nodescr_stride = L.nodescr_stride;
   m.nodescr = L.nodescr_in_smem
                   ? base + L.nodescr
-                  : nodescr_g + (size_t)blockIdx.x * kWarps * L.nodescr_stride;
+                  : nodescr_g + (size_t)blockIdx.x * (blockDim.x >> 5) * L.nodescr_stride;
   return m;
 }
 
@@ -108,8 +108,8 @@ __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int lev
   const int nmov = (level == L) ? 0 : (1 << (L - level - 1));
   const int ord0 = (level == L) ? 0 : (1 << (L - level - 1)) - 1;
   const int sp = species_of(s, ipart);
-  const double sigma = 1.0 * sqrt(s.lambda[sp] * s.tau * nStride);
-  const double inv2Sigma2 = 0.5 / (sigma * sigma);
+  const double sigma = s.mov_sigma[level][sp];
+  const double inv2Sigma2 = s.mov_inv2s2[level][sp];
   double part = 0.0;
   for (int k = threadIdx.x; k < nmov; k += blockDim.x) {
     const int t = nStride * (2 * k + 1), tp = t - nStride, tn = t + nStride;
@@ -208,7 +208,7 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
     int start = 0;
     for (int round = 0; round < 64; ++round) {
       const double sc = scale[sp];
-      for (int t = start + warp; t < nsec; t += kWarps) {
+      for (int t = start + warp; t < nsec; t += (int)(blockDim.x >> 5)) {
         SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
         SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
         double det;
@@ -292,7 +292,7 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
   const int ntask = (nsec - 1 - nStride / 2) / nStride + 1;
-  for (int task = warp; task < ntask; task += kWarps) {
+  for (int task = warp; task < ntask; task += (int)(blockDim.x >> 5)) {
     const int t = nStride / 2 + task * nStride;
     SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
     SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
@@ -493,8 +493,8 @@ __device__ double link_utau(const DevSys& s, const double* path, int ip, int t) 
   const double om = s.sho_omega[sp];
   if (om > 0) {
     const double m = s.mass[sp];
-    const double wt = om * tau, sinhwt = sinh(wt), coshwt = cosh(wt);
-    const double cschwt = 1.0 / sinhwt, cothwt = coshwt * cschwt, tin = 1.0 / tau;
+    const double coshwt = s.sho_cosh0[sp], cschwt = s.sho_csch[sp], cothwt = s.sho_coth[sp];
+    const double tin = 1.0 / tau;
     const double r0r0 = b0[0] * b0[0] + b0[1] * b0[1] + b0[2] * b0[2];
     const double r1r1 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
     const double r0r1 = b0[0] * b1[0] + b0[1] * b1[1] + b0[2] * b1[2];

@@ -11,7 +11,8 @@ namespace pimc {
 constexpr int kMaxSpecies = 4;
 constexpr int kMaxTables = 10;
 constexpr int kMaxNs = 32;  // particles per node-model species
-constexpr int kBlock = 256;
+constexpr int kMaxLevels = 8;  // levels 0..nlevel+1
+constexpr int kBlock = 256;    // largest block; engines pick 64..256 threads
 constexpr int kWarps = kBlock / 32;
 
 struct DevTable {
@@ -33,8 +34,17 @@ struct DevSys {
   double pg_nome[kMaxSpecies][3], pg_pref[kMaxSpecies][3], pg_k[kMaxSpecies][3];
   int pg_nmax[kMaxSpecies][3];
   double tau;
+  // Per-level constants, evaluated on the host with the reference's expressions
+  // (src/action/SpringAction.cc:72, src/advancer/mover/FreeMover.cc:78-79,
+  // src/action/SHOAction.cc:31-36,77-82), so no thread repeats them.
+  double spr_inv2s2[kMaxLevels][kMaxSpecies];
+  double mov_sigma[kMaxLevels][kMaxSpecies], mov_inv2s2[kMaxLevels][kMaxSpecies];
+  double sho_cosh[kMaxLevels][kMaxSpecies], sho_div1[kMaxLevels][kMaxSpecies];
+  double sho_div2[kMaxLevels];
+  double sho_coth[kMaxSpecies], sho_csch[kMaxSpecies], sho_cosh0[kMaxSpecies];
   double cell[3], cellb[3], rcut2;
   int spring, coulomb, ewald, mover, fixed_node;
+  int mixed;  // PIMC_PREC_MIXED: pair-action terms in FP32, accumulated in FP64
   double epsilon;
   int ntab;
   DevTable tab[kMaxTables];
@@ -184,12 +194,13 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 // Deterministic block sum of one double per thread (fixed tree order).
 __device__ __forceinline__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (nw == 1) return __shfl_sync(0xffffffffu, v, 0);
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
   if (w == 0) {
-    v = (l < kWarps) ? red[l] : 0.0;
+    v = (l < nw) ? red[l] : 0.0;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (l == 0) red[kWarps] = v;
   }

@@ -290,16 +290,10 @@ __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int 
   }();
   double acc = 0.0;
   // spring + SHO + PrimSHO: one item per link k (slices (k-1)*nStride, k*nStride)
-  const double lam = s.lambda[sp];
-  const double inv2Sigma2 = 0.25 / (lam * s.tau * nStride);
+  const double inv2Sigma2 = s.spr_inv2s2[level][sp];
   const double om = s.sho_omega[sp];
-  double coshwt = 0, div1 = 0, div2 = 0, msho = s.mass[sp];
-  if (om > 0) {
-    const double wt = om * s.tau * nStride;
-    coshwt = cosh(wt);
-    div1 = 1.0 / (2.0 * sinh(wt));
-    div2 = 1.0 / (2.0 * s.tau * nStride);
-  }
+  const double coshwt = s.sho_cosh[level][sp], div1 = s.sho_div1[level][sp];
+  const double div2 = s.sho_div2[level], msho = s.mass[sp];
   const bool prim = s.prim_a[sp] != 0 || s.prim_b[sp] != 0;
   // Pair tables the moving particle takes part in, and their partner ranges.
   int tb[kMaxTables], tjb[kMaxTables], tn[kMaxTables], nt = 0;
@@ -382,35 +376,36 @@ __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int 
     const double pjx1 = m.s1x[t1 * np + j], pjy1 = m.s1y[t1 * np + j], pjz1 = m.s1z[t1 * np + j];
     const double pjx0 = m.s1x[t0 * np + j], pjy0 = m.s1y[t0 * np + j], pjz0 = m.s1z[t0 * np + j];
     const bool offdiag = level < 3 && t.norder > 0;
-    double act[2];
+    if (s.mixed) {
+      // FP32 pair terms (the O(N) part), their difference accumulated in FP64.
+      float actf[2];
 #pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {
-      double ax, ay, az, bx, by, bz;
-      if (pass == 0) {
-        ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
-        bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
-      } else {
-        ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
-        bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
+      for (int pass = 0; pass < 2; ++pass) {
+        double ax, ay, az, bx, by, bz;
+        if (pass == 0) {
+          ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
+          bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
+        } else {
+          ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
+          bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
+        }
+        double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
+        pbc(s, dx, dy, dz);
+        double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
+        pbc(s, px, py, pz);
+        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+        const float gx = (float)px, gy = (float)py, gz = (float)pz;
+        const float r = sqrtf(fx * fx + fy * fy + fz * fz);
+        const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
+        const float qq = 0.5f * (r + rp);
+        const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
+        const float s2 = offdiag ? __fdividef(sx * sx + sy * sy + sz * sz, qq * qq) : 0.f;
+        actf[pass] = tab_uk0_f(t, qq, s2, offdiag ? t.norder : 0) * (float)nStride;
       }
-      double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
-      pbc(s, dx, dy, dz);
-      double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
-      pbc(s, px, py, pz);
-      const double r = sqrt(dot3(dx, dy, dz, dx, dy, dz));
-      const double rp = sqrt(dot3(px, py, pz, px, py, pz));
-      const double qq = 0.5 * (r + rp);
-      double a;
-      if (offdiag) {
-        const double sx = dx - px, sy = dy - py, sz = dz - pz;
-        const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (qq * qq);
-        a = tab_uk0(t, qq, s2) * nStride;
-      } else {
-        a = tab_u00(t, qq) * nStride;
-      }
-      act[pass] = a;
+      acc += (double)(actf[0] - actf[1]);
+      continue;
     }
-    acc += act[0] - act[1];
+    double act[2];    acc += act[0] - act[1];
   }
   return acc;
 }
