@@ -405,7 +405,35 @@ __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int 
       acc += (double)(actf[0] - actf[1]);
       continue;
     }
-    double act[2];    acc += act[0] - act[1];
+    double act[2];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      double ax, ay, az, bx, by, bz;
+      if (pass == 0) {
+        ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
+        bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
+      } else {
+        ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
+        bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
+      }
+      double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
+      pbc(s, dx, dy, dz);
+      double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
+      pbc(s, px, py, pz);
+      const double r = sqrt(dot3(dx, dy, dz, dx, dy, dz));
+      const double rp = sqrt(dot3(px, py, pz, px, py, pz));
+      const double qq = 0.5 * (r + rp);
+      double a;
+      if (offdiag) {
+        const double sx = dx - px, sy = dy - py, sz = dz - pz;
+        const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (qq * qq);
+        a = tab_uk0(t, qq, s2) * nStride;
+      } else {
+        a = tab_u00(t, qq) * nStride;
+      }
+      act[pass] = a;
+    }
+    acc += act[0] - act[1];
   }
   return acc;
 }
