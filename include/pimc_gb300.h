@@ -202,6 +202,27 @@ int pimc_node_evaluate(pimc_engine* e, int ispec, int nbatch, const double* r1,
                        const double* r2, double* det, double* d1, double* d2, int* err);
 int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale);
 
+/* ---- allocation-free NodeModel-level entry point ------------------------ */
+
+/* The same node-model evaluation as pimc_node_evaluate, for callers that
+ * cannot allocate GPU memory: host code that runs inside another framework's
+ * memory budget or pool, or that must not call cudaMalloc/cudaFree on a
+ * latency-critical path.  No engine is needed and nothing is allocated: sys is
+ * read by value, r1/r2 ([nbatch][npart][3]) and det/err ([nbatch]),
+ * d1/d2 ([nbatch][npart]) are the caller's DEVICE buffers, the Slater-matrix
+ * scratch is a fixed 3 MiB static device array (128 slots of 3*32*32 doubles),
+ * and the kernel is issued on `stream` (cudaStream_t, NULL = legacy default).
+ * scale is the node model's current scale (pimc_node_scale).  Limits: node
+ * species of at most 32 particles, npart <= 1024; larger sizes return
+ * PIMC_ERR_CAPACITY.  The first call on a device looks up the scratch array's
+ * device address on that device, so make it before any stream capture.  Every
+ * call shares the one scratch array: calls that overlap on the GPU race and
+ * must be ordered by the caller (one stream, or events).  Asynchronous.
+ * This entry point has no counterpart in the reference. */
+int pimc_node_evaluate_noalloc(const pimc_system* sys, int ispec, double scale, int nbatch,
+                               const double* r1, const double* r2, double* det, double* d1,
+                               double* d2, int* err, void* stream);
+
 /* ---- random streams ---------------------------------------------------- */
 
 /* The first n uniforms and n normals of replica `replica`'s attempt `attempt`

@@ -708,4 +708,50 @@ int pimc_fp64_peak(double* tflops) {
 
 int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
 
+// Allocation-free node evaluation.  The device address of the static scratch
+// array is looked up once per device (cudaGetSymbolAddress, with that device
+// current) on the first call made on it, and cached.
+namespace {
+constexpr int kMaxDevices = 64;
+double* g_noalloc_addr[kMaxDevices] = {nullptr};
+}  // namespace
+
+int pimc_node_evaluate_noalloc(const pimc_system* sys, int ispec, double scale, int nbatch,
+                               const double* r1, const double* r2, double* det, double* d1,
+                               double* d2, int* err, void* stream) {
+  if (!sys || nbatch <= 0 || !r1 || !r2 || !det || !d1 || !d2 || !err)
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  if (int rc = validate(*sys)) return rc;
+  if (ispec < 0 || ispec >= sys->nspecies || !sys->node_kind[ispec])
+    return fail(PIMC_ERR_INVALID, "species has no node model");
+  if (sys->spec_count[ispec] > kMaxNs)
+    return fail(PIMC_ERR_CAPACITY, "node species larger than 32 particles (scratch slot limit)");
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(PIMC_ERR_CAPACITY, "device ordinal beyond 63");
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = (double*)p;
+  }
+  NoAllocParams P;
+  fill_sys(*sys, P.sys);
+  P.r1 = r1;
+  P.r2 = r2;
+  P.det = det;
+  P.d1 = d1;
+  P.d2 = d2;
+  P.err = err;
+  P.scale = scale;
+  P.ispec = ispec;
+  P.nbatch = nbatch;
+  P.scratch = g_noalloc_addr[dev];
+  const int grid = nbatch < kNoAllocSlots ? nbatch : kNoAllocSlots;
+  const size_t smem = 6 * (size_t)sys->npart * sizeof(double);
+  if (smem > 48 * 1024) return fail(PIMC_ERR_CAPACITY, "npart beyond 1024");
+  node_eval_noalloc_kernel<<<grid, 32, smem, (cudaStream_t)stream>>>(P);
+  CU(cudaGetLastError());
+  return PIMC_OK;
+}
+
 }  // extern "C"

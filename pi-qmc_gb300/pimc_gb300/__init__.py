@@ -120,6 +120,8 @@ def lib():
         L.pimc_node_scale.argtypes = [P, I, I, D]
         L.pimc_stream_sample.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, I, D, D]
         L.pimc_fp64_peak.argtypes = [D]
+        L.pimc_node_evaluate_noalloc.argtypes = [C.POINTER(System), I, C.c_double, I, P, P, P,
+                                                 P, P, P, P]
         L.pimc_kernel_launches.argtypes = [P]
         L.pimc_kernel_launches.restype = C.c_int64
         _lib = L
