@@ -4,7 +4,9 @@ Workload (default): the fixed-node harmonic dot — 20 electrons (10 up, 10
 down), SHONodes free-oscillator nodes (two 10x10 Slater determinants per
 slice), beta=20, M=1024 slices, bisection level 5, Coulomb pair action
 (norder 3), omega=1 — run as R independent replicas (clones) of that system on
-one GPU.  One step = `--attempts` section-move attempts on every replica.
+one GPU.  One step = the body of pi-qmc's main loop: one sweep of section-move
+attempts on every replica (ceil(M/2^L) * N = 640 attempts; `--attempts`
+overrides) followed by one thermodynamic-energy measurement of every replica.
 One attempted bead-update = one interior bead proposed by a bisection move,
 nmoving*(2^L-1) = 31 per attempt, counted whether or not a level rejects.
 
@@ -62,8 +64,14 @@ def init_kind(name):
 
 
 def defaults(name):
-    # replicas per GPU and attempts per replica per step
-    return {"dot20_fn": (1216, 16), "dot2": (9728, 64), "heg54": (152, 1)}[name]
+    # replicas per GPU and attempts per replica per step (0: one sweep)
+    return {"dot20_fn": (608, 0), "dot2": (9728, 0), "heg54": (152, 1)}[name]
+
+
+def sweep_attempts(kw):
+    """Section attempts in one sweep: ceil(M / 2^L) sections times N particles."""
+    L = kw["nlevel"]
+    return -(-kw["nslice"] // (1 << L)) * sum(kw["counts"])
 
 
 # ---------------------------------------------------------------- flop model
@@ -168,10 +176,12 @@ def _cpu_worker(args):
     else:
         sim = O.PortOracle(cfg, tabs, ew)
     sim.set_path(WL.initial_path(cfg, init_kind_for(kw), seed=seed + replica))
+    # pi-qmc's loop body: a sweep of section moves, then one energy measurement
+    chunk = sweep_attempts(kw)
     n, t0 = 0, time.perf_counter()
-    chunk = 8
     while time.perf_counter() - t0 < seconds:
         sim.run(chunk, first_attempt=n)
+        sim.thermo_energy()
         n += chunk
     dt = time.perf_counter() - t0
     return n, dt
@@ -209,7 +219,7 @@ def run_engine(args, rank, world):
     kw = workload_kw(args.workload)
     R0, A0 = defaults(args.workload)
     R = args.replicas or R0
-    A = args.attempts or A0
+    A = args.attempts or A0 or sweep_attempts(kw)
     L = kw["nlevel"]
     prec = pimc_gb300.PIMC_PREC_MIXED if args.precision == "mixed" else pimc_gb300.PIMC_PREC_FP64
     tabs, ew = pimc_gb300.coulomb_tables(kw)
@@ -233,6 +243,7 @@ def run_engine(args, rank, world):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         eng.run_sections(A)
+        energy = eng.thermo_energy()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -245,6 +256,7 @@ def run_engine(args, rank, world):
             flush.fill_(float(i))
             ev[i][0].record(stream)
             eng.run_sections(A)
+            energy = eng.thermo_energy()
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     launches = eng.kernel_launches - n_launch0
@@ -278,6 +290,8 @@ def run_engine(args, rank, world):
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded initial paths; Philox4x32-10 proposals)",
         "config": {"workload": f"{args.workload}: " + describe(args.workload),
+                   "step": "one sweep of section moves per replica + one thermodynamic "
+                           "energy measurement per replica",
                    "replicas_per_gpu": R, "attempts_per_replica_per_step": A,
                    "bead_updates_per_attempt": (1 << L) - 1, "precision": args.precision,
                    "l2": "paths (%.0f MB) exceed L2 and a 256 MB buffer is written between steps"

@@ -210,7 +210,7 @@ int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale);
  * latency-critical path.  No engine is needed and nothing is allocated: sys is
  * read by value, r1/r2 ([nbatch][npart][3]) and det/err ([nbatch]),
  * d1/d2 ([nbatch][npart]) are the caller's DEVICE buffers, the Slater-matrix
- * scratch is a fixed 3 MiB static device array (128 slots of 3*32*32 doubles),
+ * scratch is a fixed 3.1 MiB static device array (128 slots of 3136 doubles),
  * and the kernel is issued on `stream` (cudaStream_t, NULL = legacy default).
  * scale is the node model's current scale (pimc_node_scale).  Limits: node
  * species of at most 32 particles, npart <= 1024; larger sizes return

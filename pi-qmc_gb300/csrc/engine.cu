@@ -241,7 +241,18 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
   L.ndist = take(fixed ? nsec * 2 * nsm : 0);
   L.ewt = take(ewt);
   L.ictl = take((C_NCTL + nsec + 1) / 2 + 1);
-  L.nodescr_stride = fixed ? ((3 * nsm * nsm + 1) & ~1) : 0;
+  bool sho = false;
+  for (const DevSys& d : sys)
+    for (int i = 0; i < d.nspecies; ++i) sho |= d.node_kind[i] == PIMC_NODES_SHO;
+  // exp-matrix cache of the moving species' section slices; left out (the
+  // levels then recompute whole matrices) when it would not fit
+  L.ecache = (sho && (off + nsec * nsm * nsm) * 8 <= 120 * 1024) ? take(nsec * nsm * nsm) : -1;
+  // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n) doubles
+  int stride = 0;
+  if (fixed)
+    for (int n = 1; n <= nsm; ++n)
+      stride = std::max(stride, (32 / node_group_width(n)) * node_group_scratch(n));
+  L.nodescr_stride = (stride + 1) & ~1;
   const int need = off + nwarps * L.nodescr_stride;
   const int limit = 200 * 1024 / 8;
   if (need <= limit) {
@@ -648,7 +659,7 @@ int pimc_node_evaluate(pimc_engine* e, int ispec, int nbatch, const double* r1, 
   P.err = d_err;
   P.ispec = ispec;
   P.lay = e->lay;
-  const int smem = (8 * np + 3 * n * n + 2) * 8;
+  const int smem = (8 * np + node_group_scratch(n) + 2) * 8;
   cudaFuncSetAttribute(node_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   node_eval_kernel<<<nbatch, kBlock, smem, e->stream>>>(P);
   e->launches++;

@@ -9,7 +9,7 @@ namespace pimc {
 // Offsets (in doubles) of the shared-memory working set; computed on the host
 // for the largest replica of a launch.
 struct Layout {
-  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl;
+  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache;
   int nodescr_in_smem;
   int nodescr_stride;
   int total;  // doubles
@@ -49,6 +49,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.ndist = base + L.ndist;
   m.ewt = base + L.ewt;
   m.ictl = (int*)(base + L.ictl);
+  m.ecache = L.ecache >= 0 ? base + L.ecache : nullptr;
   m.nodescr_stride = L.nodescr_stride;
   m.nodescr = L.nodescr_in_smem
                   ? base + L.nodescr
@@ -190,6 +191,21 @@ __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int lev
   return block_sum(part, m.red);
 }
 
+// Evaluates one slice pair per lane group (group width W from the species size).
+__device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int sp,
+                                                   const SliceView& v1, const SliceView& v2,
+                                                   double scale, double* scr, int full,
+                                                   double* ecache, int jcol, bool write,
+                                                   double& det, int& err, double* d1,
+                                                   double* d2) {
+  if (W == 8)
+    node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+  else if (W == 16)
+    node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+  else
+    node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+}
+
 // FixedNodeAction::initialize (src/fixednode/FixedNodeAction.cc:331-357) for every
 // species with a node model, reproducing NodeModel::evaluate's rescaling loop
 // (src/fixednode/SHONodes.cc:112-126): slices are evaluated in parallel at the
@@ -197,25 +213,32 @@ __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int lev
 // loop is replayed sequentially, and later slices are re-evaluated.
 __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int msp,
                                 uint32_t* status) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec;
   const int nsm = s.ns_max;
   int* errs = m.ictl + C_NCTL;  // [nsec]
-  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride;
   for (int sp = 0; sp < s.nspecies; ++sp) {
     if (!s.node_kind[sp]) continue;
+    const int n = s.spec_count[sp];
+    const int W = node_group_width(n), G = 32 / W, g = lane / W;
+    double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
     const int full = sp == msp;
+    double* ec = (full && s.node_kind[sp] == PIMC_NODES_SHO) ? m.ecache : nullptr;
     int start = 0;
     for (int round = 0; round < 64; ++round) {
       const double sc = scale[sp];
-      for (int t = start + warp; t < nsec; t += (int)(blockDim.x >> 5)) {
-        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
-        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
-        double det;
-        int err;
-        node_eval_warp(s, sp, v1, v2, sc, scr, full, det, err, m.dist + (t * 2) * nsm,
-                       m.dist + (t * 2 + 1) * nsm);
-        if (lane == 0) {
+      for (int base = start + warp * G; base < nsec; base += nwarps * G) {
+        const int t = base + g;
+        const bool act = t < nsec;
+        const int tt = act ? t : base;
+        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, tt, -1, 0, 0, 0};
+        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, tt, -1, 0, 0, 0};
+        double det = 0;
+        int err = 0;
+        node_eval_dispatch(W, s, sp, v1, v2, sc, scr, full, ec ? ec + (size_t)tt * n * n : nullptr,
+                           -1, act, det, err, m.dist + (tt * 2) * nsm,
+                           m.dist + (tt * 2 + 1) * nsm);
+        if (act && (lane & (W - 1)) == 0) {
           m.edet[t] = det;
           errs[t] = err;
         }
@@ -236,6 +259,8 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
       const int k = m.ictl[C_SCANK];
       if (k < 0) break;
       if (warp == 0) {
+        // pi-qmc's do-while rescale loop on slice k, by group 0 of warp 0
+        // (the other groups repeat it without storing).
         double det = m.edet[k];
         int err = errs[k];
         double sc2 = scale[sp];
@@ -249,11 +274,16 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
           if (fabs(det) < 1e-250)
             sc2 *= 2;
           else
-            sc2 *= pow(fabs(det), -1. / s.spec_count[sp]);
+            sc2 *= pow(fabs(det), -1. / n);
           SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, k, -1, 0, 0, 0};
           SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, k, -1, 0, 0, 0};
-          node_eval_warp(s, sp, v1, v2, sc2, scr, full, det, err, m.dist + (k * 2) * nsm,
-                         m.dist + (k * 2 + 1) * nsm);
+          double d = 0;
+          int e = 0;
+          node_eval_dispatch(W, s, sp, v1, v2, sc2, scr, full,
+                             ec ? ec + (size_t)k * n * n : nullptr, -1, g == 0, d, e,
+                             m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm);
+          det = __shfl_sync(0xffffffffu, d, 0);
+          err = __shfl_sync(0xffffffffu, e, 0);
         }
         if (lane == 0) {
           m.edet[k] = det;
@@ -285,22 +315,28 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
 // for the moving species at one level.
 __device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
                              int level) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max;
   const int nStride = 1 << (level + 1);
-  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride;
+  const int n = s.spec_count[msp];
+  const int W = node_group_width(n), G = 32 / W, g = lane / W;
+  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
+  double* ec = s.node_kind[msp] == PIMC_NODES_SHO ? m.ecache : nullptr;
+  const int jcol = ipart - s.spec_first[msp];
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
   const int ntask = (nsec - 1 - nStride / 2) / nStride + 1;
-  for (int task = warp; task < ntask; task += (int)(blockDim.x >> 5)) {
-    const int t = nStride / 2 + task * nStride;
+  for (int base = warp * G; base < ntask; base += nwarps * G) {
+    const int task = base + g;
+    const bool act = task < ntask;
+    const int t = nStride / 2 + (act ? task : base) * nStride;
     SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
     SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
-    double det;
-    int err;
-    node_eval_warp(s, msp, v1, v2, scale, scr, 1, det, err, m.ndist + (t * 2) * nsm,
-                   m.ndist + (t * 2 + 1) * nsm);
-    if (lane == 0) {
+    double det = 0;
+    int err = 0;
+    node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec ? ec + (size_t)t * n * n : nullptr,
+                       jcol, act, det, err, m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm);
+    if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
     }
@@ -308,7 +344,6 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
   __syncthreads();
   if (m.ictl[C_FLAG]) return 2e100;
   if (level != 0) return 0.0;
-  const int n = s.spec_count[msp];
   double part = 0.0;
   for (int it = threadIdx.x; it < (nsec - 1) * n; it += blockDim.x) {
     const int t = 1 + it / n, p = it % n;
@@ -531,6 +566,17 @@ __device__ double link_utau(const DevSys& s, const double* path, int ip, int t) 
         pbc(s, ex, ey, ez);
         double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
         pbc(s, px, py, pz);
+        if (s.mixed) {
+          const float fx = (float)ex, fy = (float)ey, fz = (float)ez;
+          const float gx = (float)px, gy = (float)py, gz = (float)pz;
+          const float r = sqrtf(fx * fx + fy * fy + fz * fz);
+          const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
+          const float q = 0.5f * (r + rp);
+          const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
+          const float s2 = __fdividef(sx * sx + sy * sy + sz * sz, q * q);
+          up += 0.5 * (double)tab_uk0d_tau_f(tb, q, s2);
+          continue;
+        }
         const double r = sqrt(dot3(ex, ey, ez, ex, ey, ez));
         const double rp = sqrt(dot3(px, py, pz, px, py, pz));
         const double q = 0.5 * (r + rp);
@@ -737,12 +783,12 @@ __global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, 
 namespace pimc {
 
 // ------------------------------------------- allocation-free node evaluation
-// Scratch for node_eval_noalloc_kernel: one slot of 3 * 32 * 32 doubles (the
-// LU, inverse and exp matrices of one Slater matrix of up to 32 particles) per
-// resident warp, kNoAllocSlots slots: 3 MiB, held by every GPU that loads the
-// library until the process exits.
+// Scratch for node_eval_noalloc_kernel: one slot of 3 * 32 * 32 + 33 doubles
+// (rounded up to 3136: the LU, inverse and exp matrices and pivot reciprocals
+// of one Slater matrix of up to 32 particles) per resident warp, kNoAllocSlots
+// slots: 3.1 MiB, held by every GPU that loads the library until exit.
 constexpr int kNoAllocSlots = 128;
-constexpr int kNoAllocSlot = 3 * kMaxNs * kMaxNs;
+constexpr int kNoAllocSlot = (node_group_scratch(kMaxNs) + 31) / 32 * 32;
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocSlots * kNoAllocSlot];
 
 struct NoAllocParams {

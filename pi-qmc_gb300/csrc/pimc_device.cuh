@@ -184,6 +184,27 @@ __device__ __forceinline__ float tab_uk0_f(const DevTable& t, float q, float s2,
   return a;
 }
 
+// FP32 tau derivative of the off-diagonal series (uk0CalcDerivatives' utau).
+__device__ __forceinline__ float tab_uk0d_tau_f(const DevTable& t, float q, float s2) {
+  q *= (float)t.rgridinv;
+  float x = __logf(q) * (float)t.logrratioinv;
+  int i = (int)x;
+  if (q < 1.f) {
+    i = 0;
+    x = 0.f;
+  } else if (i > t.ngpts - 2) {
+    i = t.ngpts - 2;
+    x = 1.f;
+  } else {
+    x -= i;
+  }
+  const float* g0 = t.ugrid32 + (size_t)i * 2 * t.ndata + t.ndata;
+  const float* g1 = g0 + 2 * t.ndata;
+  float a = 0.f;
+  for (int k = t.norder; k >= 0; k--) a = fmaf(a, s2, fmaf(x, __ldg(g1 + k) - __ldg(g0 + k), __ldg(g0 + k)));
+  return a;
+}
+
 // Error-free sum of two doubles (Knuth TwoSum) for compensated accumulation.
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
   s = a + b;

@@ -32,6 +32,7 @@ struct Smem {
   double* qpart;            // [npart] charges
   int* ictl;                // control words
   double* nodescr;          // per-warp node scratch (smem or global)
+  double* ecache;           // [nsec][n*n] exp matrices of the moving species (SHONodes)
   int nodescr_stride;       // doubles per warp
 };
 
@@ -67,37 +68,52 @@ struct SliceView {
 
 // ------------------------------------------------------------------ node model
 // NodeModel::evaluate (+ evaluateDistance) for one species on one slice pair,
-// executed by one warp.  Lanes own matrix rows.  LU with partial pivoting
+// executed by a group of W lanes (W = 8, 16 or 32; 32/W groups per warp each
+// take their own slice pair).  Lanes own matrix rows.  LU with partial pivoting
 // (first largest |pivot|, LAPACK dgetrf semantics), determinant from the U
 // diagonal and pivots, inverse by solving A X = I column per lane (dgetri
 // semantics), then the log-gradient nodal distances
 // (src/fixednode/SHONodes.cc:51-170, src/fixednode/FreeParticleNodes.cc:72-234).
-// full = 0: determinant only.
-__device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, const SliceView& v2,
-                               double scale, double* scr, int full, double& det_out,
-                               int& err_out, double* d1, double* d2) {
-  const int lane = threadIdx.x & 31;
+// full = 0: determinant only.  Every lane of the warp must call this (the
+// shuffles span the warp); a group with write = false computes but stores
+// nothing.  For SHONodes, ecache (n*n, or null) holds the slice's exp matrix:
+// jcol < 0 fills it, jcol >= 0 reuses it and recomputes column jcol only (the
+// other columns' inputs are unchanged, so the values are bit-identical).
+template <int W>
+__device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
+                                const SliceView& v2, double scale, double* scr, int full,
+                                double* ecache, int jcol, bool write, double& det_out,
+                                int& err_out, double* d1, double* d2) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
   const int f = s.spec_first[sp];
-  double* A = scr;          // n*n column-major, LU then scratch
-  double* X = scr + n * n;  // n*n inverse, column-major
+  double* A = scr;          // n*n column-major, LU
+  double* X = A + n * n;    // n*n inverse, column-major
   double* E = X + n * n;    // n*n exp values (SHO nodes)
+  double* R = E + n * n;    // n reciprocals of the U diagonal
   const bool sho = s.node_kind[sp] == 1;
   // --- build the Slater matrix: A(i,j) = scale * rho(r1_j, r2_i)
-  if (lane < n) {
+  if (gl < n) {
     double rix, riy, riz;
-    v2.get(f + lane, rix, riy, riz);
+    v2.get(f + gl, rix, riy, riz);
     if (sho) {
       const double c = s.node_c[sp], ch = s.node_cosh[sp];
       const double ri2 = dot3(rix, riy, riz, rix, riy, riz);
       for (int j = 0; j < n; ++j) {
-        double rjx, rjy, rjz;
-        v1.get(f + j, rjx, rjy, rjz);
-        const double rj2 = dot3(rjx, rjy, rjz, rjx, rjy, rjz);
-        const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
-        const double e = exp(-c * ((ri2 + rj2) * ch - 2.0 * rirj));
-        E[j * n + lane] = e;
-        A[j * n + lane] = scale * e;
+        double e;
+        if (ecache && jcol >= 0 && j != jcol) {
+          e = ecache[j * n + gl];
+        } else {
+          double rjx, rjy, rjz;
+          v1.get(f + j, rjx, rjy, rjz);
+          const double rj2 = dot3(rjx, rjy, rjz, rjx, rjy, rjz);
+          const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
+          e = exp(-c * ((ri2 + rj2) * ch - 2.0 * rirj));
+          if (ecache && jcol < 0 && write) ecache[j * n + gl] = e;
+        }
+        E[j * n + gl] = e;
+        A[j * n + gl] = scale * e;
       }
     } else {
       for (int j = 0; j < n; ++j) {
@@ -109,7 +125,7 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
         ear2 *= pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g);
         ear2 *= pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g);
         ear2 *= pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g);
-        A[j * n + lane] = ear2;
+        A[j * n + gl] = ear2;
       }
     }
   }
@@ -117,25 +133,26 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
   // --- LU with partial pivoting
   int info = 0;
   unsigned pivbits = 0;  // bit j set: row j was interchanged
-  int piv_lane = lane;   // piv[lane] for lane < n
+  int piv_lane = gl;     // piv[gl] for gl < n
   for (int j = 0; j < n; ++j) {
-    double av = (lane >= j && lane < n) ? fabs(A[j * n + lane]) : -1.0;
-    int ai = lane;
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ov = __shfl_down_sync(0xffffffffu, av, o);
-      const int oi = __shfl_down_sync(0xffffffffu, ai, o);
+    double av = (gl >= j && gl < n) ? fabs(A[j * n + gl]) : -1.0;
+    int ai = gl;
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+      const double ov = __shfl_down_sync(FULL, av, o, W);
+      const int oi = __shfl_down_sync(FULL, ai, o, W);
       if (ov > av || (ov == av && oi < ai)) {
         av = ov;
         ai = oi;
       }
     }
-    const int p = __shfl_sync(0xffffffffu, ai, 0);
-    if (lane == j) piv_lane = p;
+    const int p = __shfl_sync(FULL, ai, 0, W);
+    if (gl == j) piv_lane = p;
     const double apj = A[j * n + p];
     if (apj != 0.0) {
       if (p != j) {
         pivbits |= 1u << j;
-        for (int k = lane; k < n; k += 32) {
+        for (int k = gl; k < n; k += W) {
           const double t = A[k * n + j];
           A[k * n + j] = A[k * n + p];
           A[k * n + p] = t;
@@ -143,14 +160,15 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
       }
       __syncwarp();
       const double rinv = 1.0 / A[j * n + j];
-      if (lane > j && lane < n) A[j * n + lane] *= rinv;
+      if (gl == j) R[j] = rinv;
+      if (gl > j && gl < n) A[j * n + gl] *= rinv;
     } else if (info == 0) {
       info = j + 1;
     }
     __syncwarp();
-    if (lane > j && lane < n) {
-      const double lij = A[j * n + lane];
-      for (int k = j + 1; k < n; ++k) A[k * n + lane] -= lij * A[k * n + j];
+    if (gl > j && gl < n) {
+      const double lij = A[j * n + gl];
+      for (int k = j + 1; k < n; ++k) A[k * n + gl] -= lij * A[k * n + j];
     }
     __syncwarp();
   }
@@ -160,36 +178,40 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
     det *= A[i * n + i];
     det *= ((pivbits >> i) & 1u) ? -1 : 1;
   }
-  det_out = det;
-  err_out = info != 0;
-  if (!full || info != 0) return;
+  if (write) {
+    det_out = det;
+    err_out = info != 0;
+  }
+  if (!full) return;  // the same for every group of the warp
   // --- inverse: lane c solves A x = e_c
-  int pos = lane;  // e_c after the row interchanges (every lane takes part in the shuffles)
+  int pos = gl;  // e_c after the row interchanges (every lane takes part in the shuffles)
   for (int j = 0; j < n; ++j) {
-    const int pj = __shfl_sync(0xffffffffu, piv_lane, j);
+    const int pj = __shfl_sync(FULL, piv_lane, j, W);
     if (pos == j)
       pos = pj;
     else if (pos == pj)
       pos = j;
   }
-  if (lane < n) {
-    double* x = X + lane * n;
+  if (info == 0 && gl < n) {
+    double* x = X + gl * n;
     for (int i = 0; i < n; ++i) x[i] = (i == pos) ? 1.0 : 0.0;
     for (int j = pos; j < n; ++j) {
       const double xj = x[j];
       for (int i = j + 1; i < n; ++i) x[i] -= A[j * n + i] * xj;
     }
     for (int j = n - 1; j >= 0; --j) {
-      const double xj = x[j] / A[j * n + j];
+      const double xj = x[j] * R[j];
       x[j] = xj;
       for (int i = 0; i < j; ++i) x[i] -= A[j * n + i] * xj;
     }
   }
   __syncwarp();
-  // --- nodal distances.  inv(j,i) = X[i*n + j].
+  // --- nodal distances.  inv(j,i) = X[i*n + j].  (No early exit: a singular
+  // group simply skips them, so the warp stays converged.)
   const double twom_tau = 2 * s.mass[sp];
-  if (lane < n) {
-    const int j = lane;  // d1: gradient with respect to r1_j
+  const bool ok = info == 0;
+  if (ok && gl < n) {
+    const int j = gl;  // d1: gradient with respect to r1_j
     double rjx, rjy, rjz;
     v1.get(f + j, rjx, rjy, rjz);
     double lx = 0, ly = 0, lz = 0;
@@ -226,10 +248,10 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
         lz += w * gz * scale;
       }
     }
-    d1[j] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
+    if (write) d1[j] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
   }
-  if (lane < n) {
-    const int i = lane;  // d2: gradient with respect to r2_i
+  if (ok && gl < n) {
+    const int i = gl;  // d2: gradient with respect to r2_i
     double rix, riy, riz;
     v2.get(f + i, rix, riy, riz);
     double lx = 0, ly = 0, lz = 0;
@@ -266,9 +288,25 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
         lz += w * gz * scale;
       }
     }
-    d2[i] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
+    if (write) d2[i] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
   }
   __syncwarp();
+}
+
+// Scratch doubles one lane group needs for an n-particle species.
+__host__ __device__ constexpr int node_group_scratch(int n) { return 3 * n * n + n + 1; }
+
+// Group width for an n-particle species.
+__host__ __device__ __forceinline__ int node_group_width(int n) {
+  return n <= 8 ? 8 : (n <= 16 ? 16 : 32);
+}
+
+// One warp evaluates one slice pair (the entry-point kernels).
+__device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, const SliceView& v2,
+                               double scale, double* scr, int full, double& det_out,
+                               int& err_out, double* d1, double* d2) {
+  node_eval_group<32>(s, sp, v1, v2, scale, scr, full, nullptr, -1, true, det_out, err_out, d1,
+                      d2);
 }
 
 // ------------------------------------------------------------------ actions
