@@ -5,6 +5,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -64,6 +66,9 @@ struct pimc_engine {
   DevBuf<DevState> d_state;
   DevBuf<double> d_paths;
   DevBuf<double> d_nodescr;
+  DevBuf<double> d_nodecache;
+  DevBuf<int> d_order;
+  DevBuf<int> d_next;
   DevBuf<double> d_ugrid;
   DevBuf<float> d_ugrid32;
   DevBuf<int> d_kvec;
@@ -78,6 +83,9 @@ struct pimc_engine {
     d_state.free();
     d_paths.free();
     d_nodescr.free();
+    d_nodecache.free();
+    d_order.free();
+    d_next.free();
     d_ugrid.free();
     d_ugrid32.free();
     d_kvec.free();
@@ -240,13 +248,14 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
   L.dist = take(fixed ? nsec * 2 * nsm : 0);
   L.ndist = take(fixed ? nsec * 2 * nsm : 0);
   L.ewt = take(ewt);
-  L.ictl = take((C_NCTL + nsec + 1) / 2 + 1);
+  L.ictl = take((C_NCTL + 2 * nsec + 1) / 2 + 1);
   bool sho = false;
   for (const DevSys& d : sys)
     for (int i = 0; i < d.nspecies; ++i) sho |= d.node_kind[i] == PIMC_NODES_SHO;
   // exp-matrix cache of the moving species' section slices; left out (the
   // levels then recompute whole matrices) when it would not fit
   L.ecache = (sho && (off + nsec * nsm * nsm) * 8 <= 120 * 1024) ? take(nsec * nsm * nsm) : -1;
+  L.ncol = fixed ? take(nsec * nsm) : -1;
   // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n) doubles
   int stride = 0;
   if (fixed)
@@ -303,6 +312,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
     size_t pool_off;
   };
   std::vector<Pending> pend;
+  std::map<const double*, size_t> pooled;
   for (int r = 0; r < nrep; ++r) {
     const pimc_system& s = uniform ? sys[0] : sys[r];
     if (int rc = validate(s)) {
@@ -338,12 +348,14 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
         dt.npart2 = d.spec_count[t.species2];
         dt.rgridinv = t.rgridinv;
         dt.logrratioinv = t.logrratioinv;
-        // share identical tables between replicas of one system
+        // one device copy per distinct host table (replicas of a batch share them)
         size_t po = pool.size();
-        if (uniform && r > 0) {
-          po = (size_t)pend[k - t0].pool_off;
+        auto hit = pooled.find(t.ugrid);
+        if (hit != pooled.end()) {
+          po = hit->second;
         } else {
           pool.insert(pool.end(), t.ugrid, t.ugrid + (size_t)t.ngpts * 2 * dt.ndata);
+          pooled[t.ugrid] = po;
         }
         pend.push_back({r, d.ntab, po});
         d.ntab++;
@@ -435,15 +447,59 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   } else {
     for (DevSys& d : e->hsys) d.inv_offset = -1;
   }
+  // Slater-result cache: per replica, per species, per path slice.  Left out
+  // when the two sections of an attempt can overlap (2^L >= M/2).
+  {
+    long long coff = 0;
+    for (DevSys& d : e->hsys) {
+      const bool use = d.fixed_node && (1 << d.nlevel) < d.nslice / 2;
+      d.nc_stride = (2 + 2 * d.ns_max + d.ns_max * d.ns_max + 1) & ~1;
+      if (use) {
+        d.nc_offset = coff;
+        coff += (long long)d.nspecies * d.nslice * d.nc_stride;
+      } else {
+        d.nc_offset = -1;
+      }
+    }
+    if (coff > 0) {
+      if (e->d_nodecache.alloc(coff)) {
+        delete e;
+        return fail(PIMC_ERR_CUDA, "cudaMalloc node cache");
+      }
+      cudaMemset(e->d_nodecache.p, 0xff, coff * sizeof(double));  // NaN epochs: all invalid
+    }
+  }
   if (e->d_sys.alloc(nrep) || e->d_state.alloc(nrep) || e->d_paths.alloc(off)) {
     delete e;
     return fail(PIMC_ERR_CUDA, "cudaMalloc engine state");
   }
   cudaMemcpy(e->d_sys.p, e->hsys.data(), nrep * sizeof(DevSys), cudaMemcpyHostToDevice);
+  {
+    // longest-processing-time-first order of the work queue
+    std::vector<double> cost(nrep);
+    for (int r = 0; r < nrep; ++r) {
+      const DevSys& d = e->hsys[r];
+      double c = (double)d.npart * d.npart;
+      for (int i = 0; i < d.nspecies; ++i)
+        if (d.node_kind[i]) c += 2.0 * d.spec_count[i] * d.spec_count[i] * (d.spec_count[i] + 20);
+      cost[r] = c * ((1 << d.nlevel) + 1);
+    }
+    std::vector<int> order(nrep);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    if (e->d_order.alloc(nrep) || e->d_next.alloc(1)) {
+      delete e;
+      return fail(PIMC_ERR_CUDA, "cudaMalloc work queue");
+    }
+    cudaMemcpy(e->d_order.p, order.data(), nrep * sizeof(int), cudaMemcpyHostToDevice);
+  }
   std::vector<DevState> st(nrep);
   for (DevState& x : st) {
     memset(&x, 0, sizeof(x));
-    for (int k = 0; k < kMaxSpecies; ++k) x.node_scale[k] = 1.0;
+    for (int k = 0; k < kMaxSpecies; ++k) {
+      x.node_scale[k] = 1.0;
+      x.epoch[k] = 0;
+    }
   }
   cudaMemcpy(e->d_state.p, st.data(), nrep * sizeof(DevState), cudaMemcpyHostToDevice);
   cudaMemset(e->d_paths.p, 0, off * sizeof(double));
@@ -490,6 +546,8 @@ int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (!e || !host_xyz) return fail(PIMC_ERR_INVALID, "null argument");
   CU(cudaMemcpyAsync(e->d_paths.p, host_xyz, e->path_off[e->nrep] * sizeof(double),
                      cudaMemcpyHostToDevice, e->stream));
+  if (e->d_nodecache.p)  // new paths: every cached Slater result is stale
+    CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double), e->stream));
   return PIMC_OK;
 }
 
@@ -520,7 +578,11 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
   P.state = e->d_state.p;
   P.paths = e->d_paths.p;
   P.nodescr_g = e->d_nodescr.p;
+  P.nodecache = e->d_nodecache.p;
   P.rec = d_rec;
+  P.order = e->d_order.p;
+  P.next = e->d_next.p;
+  CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
   P.nattempt = nattempt;
   P.nrep = e->nrep;
   P.seed = e->seed;

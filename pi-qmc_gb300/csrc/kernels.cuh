@@ -9,7 +9,7 @@ namespace pimc {
 // Offsets (in doubles) of the shared-memory working set; computed on the host
 // for the largest replica of a launch.
 struct Layout {
-  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache;
+  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
   int nodescr_in_smem;
   int nodescr_stride;
   int total;  // doubles
@@ -19,8 +19,11 @@ struct RunParams {
   const DevSys* sys;
   DevState* state;
   double* paths;
+  double* nodecache;  // per-replica Slater-result cache pool (null: none)
   double* nodescr_g;  // global per-warp node scratch when it does not fit in smem
   pimc_move_record* rec;
+  const int* order;  // replicas in decreasing cost (longest first)
+  int* next;         // work-queue head, zeroed before each launch
   int nattempt;
   int nrep;
   uint64_t seed;
@@ -50,6 +53,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.ewt = base + L.ewt;
   m.ictl = (int*)(base + L.ictl);
   m.ecache = L.ecache >= 0 ? base + L.ecache : nullptr;
+  m.ncol = L.ncol >= 0 ? base + L.ncol : nullptr;
   m.nodescr_stride = L.nodescr_stride;
   m.nodescr = L.nodescr_in_smem
                   ? base + L.nodescr
@@ -197,13 +201,26 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
                                                    double scale, double* scr, int full,
                                                    double* ecache, int jcol, bool write,
                                                    double& det, int& err, double* d1,
-                                                   double* d2) {
+                                                   double* d2, double* newcol = nullptr) {
   if (W == 8)
-    node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+    node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
+                       newcol);
   else if (W == 16)
-    node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+    node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
+                        newcol);
   else
-    node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2);
+    node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
+                        newcol);
+}
+
+// Slater-result cache entry of species sp for path slice t1 (r1 at t1, r2 at
+// t1 + M/2): [0] epoch (NaN = invalid), [1] determinant, [2..2+n) d1,
+// [2+n..2+2n) d2, [2+2n..) exp matrix (SHONodes).  An entry is valid while
+// neither slice's particles of that species have moved and the species'
+// scale epoch is unchanged; evaluate() of the same inputs at the same scale
+// returns exactly these values, so a hit replaces the evaluation bit for bit.
+__device__ __forceinline__ double* cache_entry(const DevSys& s, double* cache, int sp, int t1) {
+  return cache + ((size_t)sp * s.nslice + t1) * s.nc_stride;
 }
 
 // FixedNodeAction::initialize (src/fixednode/FixedNodeAction.cc:331-357) for every
@@ -211,36 +228,73 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
 // (src/fixednode/SHONodes.cc:112-126): slices are evaluated in parallel at the
 // current scale; at the first slice whose determinant leaves [1e-50, 1e50] the
 // loop is replayed sequentially, and later slices are re-evaluated.
-__device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int msp,
-                                uint32_t* status) {
+__device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
+                                int msp, uint32_t* status, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int nsec = s.nsec;
+  const int nsec = s.nsec, M = s.nslice;
   const int nsm = s.ns_max;
-  int* errs = m.ictl + C_NCTL;  // [nsec]
+  int* errs = m.ictl + C_NCTL;          // [nsec]
+  int* miss = m.ictl + C_NCTL + nsec;   // [nsec]
+  const double NaN = __longlong_as_double(0x7ff8000000000000LL);
   for (int sp = 0; sp < s.nspecies; ++sp) {
     if (!s.node_kind[sp]) continue;
     const int n = s.spec_count[sp];
-    const int W = node_group_width(n), G = 32 / W, g = lane / W;
+    const int W = node_group_width(n), G = 32 / W, g = lane / W, gl = lane & (W - 1);
     double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
-    const int full = sp == msp;
-    double* ec = (full && s.node_kind[sp] == PIMC_NODES_SHO) ? m.ecache : nullptr;
+    const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
+    const bool mine = sp == msp;
     int start = 0;
     for (int round = 0; round < 64; ++round) {
       const double sc = scale[sp];
-      for (int base = start + warp * G; base < nsec; base += nwarps * G) {
-        const int t = base + g;
-        const bool act = t < nsec;
-        const int tt = act ? t : base;
-        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, tt, -1, 0, 0, 0};
-        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, tt, -1, 0, 0, 0};
+      const double ep = (double)epoch[sp];
+      // hits: copy cached results; misses: list them
+      if (threadIdx.x == 0) m.ictl[C_NMISS] = 0;
+      __syncthreads();
+      for (int t = start + (int)threadIdx.x; t < nsec; t += blockDim.x) {
+        const double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
+        if (e && e[0] == ep) {
+          m.edet[t] = e[1];
+          errs[t] = 0;
+          if (mine)
+            for (int j = 0; j < n; ++j) {
+              m.dist[(t * 2) * nsm + j] = e[2 + j];
+              m.dist[(t * 2 + 1) * nsm + j] = e[2 + n + j];
+            }
+        } else {
+          miss[atomicAdd(&m.ictl[C_NMISS], 1)] = t;
+        }
+      }
+      __syncthreads();
+      const int nmiss = m.ictl[C_NMISS];
+      for (int base = warp * G; base < nmiss; base += nwarps * G) {
+        const int task = base + g;
+        const bool act = task < nmiss;
+        const int t = miss[act ? task : base];
+        double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
+        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
+        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
         double det = 0;
         int err = 0;
-        node_eval_dispatch(W, s, sp, v1, v2, sc, scr, full, ec ? ec + (size_t)tt * n * n : nullptr,
-                           -1, act, det, err, m.dist + (tt * 2) * nsm,
-                           m.dist + (tt * 2 + 1) * nsm);
-        if (act && (lane & (W - 1)) == 0) {
-          m.edet[t] = det;
-          errs[t] = err;
+        double* ec = sho ? (e ? e + 2 + 2 * n : (mine ? m.ecache + (size_t)t * n * n : nullptr))
+                         : nullptr;
+        // with a cache every miss is evaluated in full so that its entry is complete
+        const int full = (mine || e) ? 1 : 0;
+        double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
+        double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
+        node_eval_dispatch(W, s, sp, v1, v2, sc, scr, full, ec, -1, act, det, err, d1, d2);
+        if (act) {
+          if (e && mine && gl < n) {
+            e[2 + gl] = d1[gl];
+            e[2 + n + gl] = d2[gl];
+          }
+          if (gl == 0) {
+            m.edet[t] = det;
+            errs[t] = err;
+            if (e) {
+              e[1] = det;
+              e[0] = err ? NaN : ep;
+            }
+          }
         }
       }
       __syncthreads();
@@ -265,6 +319,7 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
         int err = errs[k];
         double sc2 = scale[sp];
         int guard = 0;
+        double* dsc = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
         while (err || fabs(det) < 1e-50 || fabs(det) > 1e50) {
           if (err || ++guard > 2000) {
             if (lane == 0) *status |= err ? (PIMC_STATUS_SINGULAR | PIMC_STATUS_RESCALE_LIMIT)
@@ -278,17 +333,21 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
           SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, k, -1, 0, 0, 0};
           SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, k, -1, 0, 0, 0};
           double d = 0;
-          int e = 0;
-          node_eval_dispatch(W, s, sp, v1, v2, sc2, scr, full,
-                             ec ? ec + (size_t)k * n * n : nullptr, -1, g == 0, d, e,
-                             m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm);
+          int e2 = 0;
+          double* ec = (sho && mine) ? m.ecache + (size_t)k * n * n : nullptr;
+          if (!m.ecache) ec = nullptr;
+          node_eval_dispatch(W, s, sp, v1, v2, sc2, dsc, mine ? 1 : 0, nullptr, -1, g == 0, d,
+                             e2, m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm);
+          (void)ec;
           det = __shfl_sync(0xffffffffu, d, 0);
-          err = __shfl_sync(0xffffffffu, e, 0);
+          err = __shfl_sync(0xffffffffu, e2, 0);
         }
         if (lane == 0) {
           m.edet[k] = det;
           errs[k] = err;
+          if (sc2 != scale[sp]) epoch[sp] += 1;
           scale[sp] = sc2;
+          if (cache) cache_entry(s, cache, sp, wrap_slice(ifirst1 + k, M))[0] = NaN;
         }
       }
       __syncthreads();
@@ -314,14 +373,14 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
 // FixedNodeAction::getActionDifference (src/fixednode/FixedNodeAction.cc:39-131)
 // for the moving species at one level.
 __device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
-                             int level) {
+                             int level, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max;
   const int nStride = 1 << (level + 1);
   const int n = s.spec_count[msp];
   const int W = node_group_width(n), G = 32 / W, g = lane / W;
   double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
-  double* ec = s.node_kind[msp] == PIMC_NODES_SHO ? m.ecache : nullptr;
+  const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
   const int jcol = ipart - s.spec_first[msp];
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
@@ -334,8 +393,16 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
     SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
     double det = 0;
     int err = 0;
-    node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec ? ec + (size_t)t * n * n : nullptr,
-                       jcol, act, det, err, m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm);
+    double* ec = nullptr;
+    if (sho) {
+      if (cache)
+        ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
+      else if (m.ecache)
+        ec = m.ecache + (size_t)t * n * n;
+    }
+    node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
+                       m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
+                       (sho && cache) ? m.ncol + t * nsm : nullptr);
     if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
@@ -374,9 +441,20 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
   extern __shared__ double smem[];
   __shared__ DevSys S;
   __shared__ double scale[kMaxSpecies];
+  __shared__ int epoch[kMaxSpecies];
   __shared__ uint32_t status;
   __shared__ long long nacc;
-  for (int r = blockIdx.x; r < P.nrep; r += gridDim.x) {
+  __shared__ int rnext;
+  // Persistent CTAs take replicas from a queue ordered longest-first, so that
+  // uneven replicas (different N, M, L) balance across the SMs.
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int k = atomicAdd(P.next, 1);
+      rnext = (k < P.nrep) ? P.order[k] : -1;
+    }
+    __syncthreads();
+    const int r = rnext;
+    if (r < 0) break;
     {
       const int* src = (const int*)(P.sys + r);
       int* dst = (int*)&S;
@@ -386,13 +464,17 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
     if (threadIdx.x == 0) {
       status = P.state[r].status;
       nacc = 0;
-      for (int k = 0; k < kMaxSpecies; ++k) scale[k] = P.state[r].node_scale[k];
+      for (int k = 0; k < kMaxSpecies; ++k) {
+        scale[k] = P.state[r].node_scale[k];
+        epoch[k] = P.state[r].epoch[k];
+      }
     }
     __syncthreads();
     const DevSys& s = S;
     Smem m = carve(smem, P.lay, s, P.nodescr_g);
     double* path = P.paths + s.path_offset;
     const uint32_t att0 = P.state[r].attempt;
+    double* cache = (P.nodecache && s.nc_offset >= 0) ? P.nodecache + s.nc_offset : nullptr;
     const int np = s.npart, nsec = s.nsec, M = s.nslice, L = s.nlevel;
     for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
     for (int a = 0; a < P.nattempt; ++a) {
@@ -433,7 +515,8 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
       }
       const int msp = species_of(s, ipart);
       const bool mynode = s.fixed_node && s.node_kind[msp];
-      if (s.fixed_node) node_initialize(s, m, scale, mynode ? msp : -1, &status);
+      if (s.fixed_node)
+        node_initialize(s, m, scale, epoch, mynode ? msp : -1, &status, cache, ifirst1);
       __syncthreads();
       pimc_move_record* rec = P.rec ? P.rec + (size_t)r * P.nattempt + a : nullptr;
       double oldDS = 0.0;
@@ -446,7 +529,7 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
           for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
         }
         double dsn = 0.0;
-        if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level);
+        if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level, cache, ifirst1);
         if (threadIdx.x == 0) {
           const double total = s.fixed_node ? ds + dsn : ds;
           const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
@@ -475,6 +558,30 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
           m.s1z[t * np + ipart] = m.mz[t];
         }
         if (threadIdx.x == 0) ++nacc;
+        if (cache && mynode) {
+          // The moved slices now hold the level evaluations; the entries that
+          // pair them the other way round (r2 on a moved slice) are stale.
+          const int n = s.spec_count[msp], jcol = ipart - s.spec_first[msp];
+          const int nsm = s.ns_max;
+          const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+          const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
+          for (int it = threadIdx.x; it < (nsec - 2) * n; it += blockDim.x) {
+            const int k = 1 + it / n, j = it % n;
+            const int t1 = wrap_slice(ifirst1 + k, M);
+            double* e = cache_entry(s, cache, msp, t1);
+            e[2 + j] = m.ndist[(k * 2) * nsm + j];
+            e[2 + n + j] = m.ndist[(k * 2 + 1) * nsm + j];
+            if (sho) e[2 + 2 * n + jcol * n + j] = m.ncol[k * nsm + j];
+          }
+          __syncthreads();
+          for (int k = 1 + threadIdx.x; k < nsec - 1; k += blockDim.x) {
+            const int t1 = wrap_slice(ifirst1 + k, M);
+            double* e = cache_entry(s, cache, msp, t1);
+            e[1] = m.ndm[k];
+            e[0] = (double)epoch[msp];
+            cache_entry(s, cache, msp, (t1 + M / 2) % M)[0] = NaN;
+          }
+        }
       }
       if (threadIdx.x == 0 && rec) {
         rec->ifirst1 = ifirst1;
@@ -502,7 +609,10 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
       P.state[r].status = status;
       P.state[r].accepted += nacc;
       P.state[r].attempted += P.nattempt;
-      for (int k = 0; k < kMaxSpecies; ++k) P.state[r].node_scale[k] = scale[k];
+      for (int k = 0; k < kMaxSpecies; ++k) {
+        P.state[r].node_scale[k] = scale[k];
+        P.state[r].epoch[k] = epoch[k];
+      }
     }
     __syncthreads();
   }

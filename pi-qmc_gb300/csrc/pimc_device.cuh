@@ -54,6 +54,8 @@ struct DevSys {
   double one_over_2v, self_energy, deltak[3];
   int ikmax[3];
   int ns_max;           // largest node-species count
+  long long nc_offset;    // doubles into the Slater-result cache pool (-1: no cache)
+  int nc_stride;          // doubles per cache entry
   long long path_offset;  // doubles into the path pool
   long long inv_offset;   // doubles into the node scratch pool (-1: shared memory)
 };
@@ -65,6 +67,7 @@ struct DevState {
   long long accepted;
   long long attempted;
   double node_scale[kMaxSpecies];
+  int epoch[kMaxSpecies];  // bumped whenever a node model's scale changes
 };
 
 // ---------------------------------------------------------------- helpers

@@ -33,11 +33,12 @@ struct Smem {
   int* ictl;                // control words
   double* nodescr;          // per-warp node scratch (smem or global)
   double* ecache;           // [nsec][n*n] exp matrices of the moving species (SHONodes)
+  double* ncol;             // [nsec][ns_max] recomputed exp column of each changed slice
   int nodescr_stride;       // doubles per warp
 };
 
 enum {
-  C_IFIRST1 = 0, C_IFIRST2, C_IPART, C_REJECT, C_FLAG, C_SCANK, C_ERRS, C_NCTL = 16
+  C_IFIRST1 = 0, C_IFIRST2, C_IPART, C_REJECT, C_FLAG, C_SCANK, C_ERRS, C_NMISS, C_NCTL = 16
 };
 
 struct SectionSizes {
@@ -83,7 +84,8 @@ template <int W>
 __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
-                                int& err_out, double* d1, double* d2) {
+                                int& err_out, double* d1, double* d2,
+                                double* newcol = nullptr) {
   constexpr unsigned FULL = 0xffffffffu;
   const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
@@ -111,6 +113,7 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
           const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
           e = exp(-c * ((ri2 + rj2) * ch - 2.0 * rirj));
           if (ecache && jcol < 0 && write) ecache[j * n + gl] = e;
+          if (newcol && j == jcol && write) newcol[gl] = e;
         }
         E[j * n + gl] = e;
         A[j * n + gl] = scale * e;

@@ -73,3 +73,43 @@ def initial_path(cfg, kind, seed=DEFAULT_SEED):
                        float) * (lbox / g) - lbox / 2 + lbox / (2 * g)
         return np.repeat(pts[None], ns, axis=0)
     raise ValueError(kind)
+
+
+def batch_dots(nrep=4096, seed=DEFAULT_SEED, levels=(4, 5), slices=(128, 256, 512, 1024),
+               nmin=2, nmax=32, omega=(0.5, 2.0), tau=1.0 / 25.6):
+    """Uneven harmonic-dot replicas: N uniform in {nmin..nmax} (ceil(N/2) up,
+    floor(N/2) down, SHONodes on each spin), omega uniform in [0.5, 2], M drawn
+    from `slices`, beta = M tau, level drawn from `levels`, Coulomb pair action.
+    The node model's temperature attribute is omega/4: at T = 1/beta the
+    free-oscillator density matrix is numerically rank-deficient in FP64 once
+    omega beta / 2 exceeds ~20 (exp(2 c r_i.r_j) rounds to 1)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nrep):
+        n = int(rng.integers(nmin, nmax + 1))
+        w = float(rng.uniform(*omega))
+        m = int(rng.choice(slices))
+        lev = int(rng.choice(levels))
+        up, dn = (n + 1) // 2, n // 2
+        counts = [up, dn] if dn > 0 else [up]
+        ns = len(counts)
+        out.append(dict(counts=counts, sho_omega=[w] * ns, nslice=m, beta=m * tau, nlevel=lev,
+                        coulomb=1, norder=3, node_kind=[1] * ns, node_omega=[w] * ns,
+                        node_temperature=w / 4.0, cell=DOT_CELL))
+    return out
+
+
+def tables_for(kw, base_tables):
+    """Pair tables of a batch replica taken from one shared table set built for
+    a two-species system with both species larger than one (same tau, masses,
+    charges and cell): pairs (0,0), (0,1), (1,1) exist as pi-qmc's CoulombAction
+    creates them (distinct species, or more than one particle)."""
+    counts = kw["counts"]
+    by = {tuple(t["species"]): t for t in base_tables}
+    out = []
+    ns = len(counts)
+    for i in range(ns):
+        for j in range(i, ns):
+            if i != j or counts[i] > 1:
+                out.append(by[(i, j)])
+    return out

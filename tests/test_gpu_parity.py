@@ -158,3 +158,53 @@ def test_kernel_launch_count(pimc):
     e.run_sections(10)
     e.run_sections(10)
     assert e.kernel_launches - n0 == 2
+
+
+@pytest.mark.parametrize("case", ["dot4_fn", "heg8"])
+def test_slater_cache_is_exact(pimc, case):
+    # Cached Slater results stand in for re-evaluations bit for bit: a chain
+    # whose cache is wiped every 25 attempts (uploading the paths invalidates
+    # it) equals an uninterrupted chain.
+    g = golden_io.load(case)
+    a = engine_for(pimc, g)
+    b = engine_for(pimc, g)
+    a.upload_paths([g["path0"]])
+    b.upload_paths([g["path0"]])
+    ra = a.run_sections(150, records=True)
+    rb = []
+    for _ in range(6):
+        rb.append(b.run_sections(25, records=True))
+        b.upload_paths(b.download_paths())
+    for k in ("reject_level", "ipart", "ifirst1"):
+        assert np.array_equal(ra[k][0], np.concatenate([r[k][0] for r in rb]))
+    assert np.array_equal(ra["ds_node"][0], np.concatenate([r["ds_node"][0] for r in rb]))
+    assert np.array_equal(a.download_paths()[0], b.download_paths()[0])
+
+
+def test_uneven_batch_matches_checker(pimc):
+    # Replicas of different N, M, L, omega in one launch (the batched form):
+    # each replica r reproduces the checker run with stream r.
+    from pimc_gb300 import workloads as WL
+    kws = WL.batch_dots(nrep=10, seed=7, levels=(3, 4), slices=(64, 128), nmax=9)
+    base, _ = pimc.coulomb_tables(dict(kws[0], counts=[2, 2], node_kind=[1, 1],
+                                       node_omega=[1.0, 1.0], sho_omega=[1.0, 1.0]))
+    tabs = [WL.tables_for(kw, base) for kw in kws]
+    eng = pimc.Engine.batch(kws, tabs, seed=99)
+    paths = [W.initial_path(O.make_config(**kw), "const", seed=500 + r)
+             for r, kw in enumerate(kws)]
+    eng.upload_paths(paths)
+    n = 120
+    rec = eng.run_sections(n, records=True)
+    out = eng.download_paths()
+    E = eng.thermo_energy()
+    for r, kw in enumerate(kws):
+        cfg = O.make_config(**dict(kw, seed=99, replica=r))
+        port = O.PortOracle(cfg, tabs[r], None)
+        port.set_path(paths[r])
+        pr = port.run(n)
+        assert np.array_equal(pr["reject_level"], rec["reject_level"][r]), r
+        assert np.array_equal(pr["ipart"], rec["ipart"][r]), r
+        assert rel_close(pr["ds"], rec["ds"][r][:, :9], 1e-12)
+        assert rel_close(pr["ds_node"], rec["ds_node"][r][:, :9], 1e-9)
+        assert np.abs(port.get_path() - out[r]).max() <= 1e-12
+        assert E[r] == pytest.approx(port.thermo_energy(), rel=1e-12)
