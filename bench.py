@@ -46,26 +46,50 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--workload", default="dot20_fn", choices=["dot20_fn", "dot2", "heg54"])
+    p.add_argument("--workload", default="dot20_fn",
+                   choices=["dot20_fn", "dot2", "heg54", "batch4096", "serve"])
     p.add_argument("--replicas", type=int, default=0, help="replicas per GPU (0: auto)")
     p.add_argument("--attempts", type=int, default=0, help="attempts per replica per step")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
+                   help="auto: the precision the workload is specified in (FP64 for dot2, "
+                        "FP32 bulk + FP64 determinants for the others)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    p.add_argument("--requests", type=int, default=2000, help="serve: requests in the stream")
+    p.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
+    p.add_argument("--sweep-scale", type=float, default=1e-5,
+                   help="serve: factor on the requested sweeps (log-uniform 1e3..1e5)")
+    p.add_argument("--slots", type=int, default=1024, help="serve: concurrent simulations")
+    p.add_argument("--pool-gb", type=float, default=32.0, help="serve: device pool for paths")
+    p.add_argument("--round-budget", type=float, default=1.0,
+                   help="serve: round length in units of 8 attempts of the largest system")
     return p.parse_args()
 
 
 def workload_kw(name):
+    if name == "serve":
+        return [kw for _, kw, _ in WL.serve_stream(64)]
+    if name == "batch4096":
+        return WL.batch_dots(4096)
     return {"dot20_fn": WL.dot20_fn, "dot2": WL.dot2, "heg54": WL.heg54}[name]()
 
 
 def init_kind(name):
-    return {"dot20_fn": "const", "dot2": "gauss", "heg54": "grid"}[name]
+    return {"dot20_fn": "const", "dot2": "gauss", "heg54": "grid", "batch4096": "const",
+            "serve": "const"}[name]
 
 
 def defaults(name):
     # replicas per GPU and attempts per replica per step (0: one sweep)
-    return {"dot20_fn": (608, 0), "dot2": (9728, 0), "heg54": (152, 1)}[name]
+    return {"dot20_fn": (608, 0), "dot2": (9728, 0), "heg54": (152, 1),
+            "batch4096": (4096, 32), "serve": (64, 64)}[name]
+
+
+def workload_precision(name, requested):
+    if requested != "auto":
+        return requested
+    return "fp64" if name == "dot2" else "mixed"
 
 
 def sweep_attempts(kw):
@@ -161,7 +185,7 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU side
 def _cpu_worker(args):
-    kw, seed, replica, seconds = args
+    kw, seed, replica, seconds, attempts = args
     # pi-qmc's constructors print progress to stdout; keep the JSON line clean
     devnull = os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)
@@ -177,14 +201,14 @@ def _cpu_worker(args):
         sim = O.PortOracle(cfg, tabs, ew)
     sim.set_path(WL.initial_path(cfg, init_kind_for(kw), seed=seed + replica))
     # pi-qmc's loop body: a sweep of section moves, then one energy measurement
-    chunk = sweep_attempts(kw)
+    chunk = attempts or sweep_attempts(kw)
     n, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
         sim.run(chunk, first_attempt=n)
         sim.thermo_energy()
         n += chunk
     dt = time.perf_counter() - t0
-    return n, dt
+    return n * ((1 << kw["nlevel"]) - 1), n, dt
 
 
 def init_kind_for(kw):
@@ -193,15 +217,17 @@ def init_kind_for(kw):
     return "const" if any(kw.get("node_kind", [0])) else "gauss"
 
 
-def cpu_throughput(kw, seconds, cores):
-    """Bead-updates/s of the CPU implementation on `cores` processes."""
+def cpu_throughput(kws, seconds, cores, attempts=0):
+    """Bead-updates/s of the CPU implementation on `cores` processes (process p
+    runs replica p of the workload)."""
+    kws = kws if isinstance(kws, list) else [kws]
     ctx = mp.get_context("spawn")
-    L = kw["nlevel"]
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(kw, 777, r, seconds) for r in range(cores)])
-    attempts = sum(n for n, _ in res)
-    wall = max(dt for _, dt in res)
-    return attempts * ((1 << L) - 1) / wall, attempts
+        res = pool.map(_cpu_worker, [(kws[r % len(kws)], 777, r, seconds, attempts)
+                                     for r in range(cores)])
+    beads = sum(b for b, _, _ in res)
+    wall = max(dt for _, _, dt in res)
+    return beads / wall, sum(n for _, n, _ in res)
 
 
 def cpu_kind():
@@ -210,40 +236,147 @@ def cpu_kind():
     return "reference" if O.RefOracle.available() else "port"
 
 
+# ---------------------------------------------------------------- serving arm
+def serve_requests(args, base, nreq, seed):
+    from pimc_gb300 import serving
+    out = []
+    for i, (t, kw, sw) in enumerate(WL.serve_stream(nreq, rate=args.rate, seed=seed,
+                                                    sweep_scale=args.sweep_scale)):
+        att = max(1, int(round(sw * WL.sweep_attempts(kw))))
+        path = WL.initial_path(kw, "const", seed=1000 + i) / math.sqrt(kw["sho_omega"][0])
+        out.append(serving.Request(i, kw, WL.tables_for(kw, base), path, att, t))
+    return out
+
+
+def run_serve(args, rank, world):
+    """Continuous batching of a Poisson stream of dot simulations: requests are
+    admitted into server slots as slots and pool memory free up, every round
+    advances each admitted simulation by its own attempts (sized so that a
+    round costs about the same device time for every system) and measures their
+    energies, and finished simulations leave.  value = bead
+    updates of all requests / wall time from the first arrival to the last
+    result; p50/p99 time-to-result per request."""
+    import torch
+    import pimc_gb300
+    from pimc_gb300 import serving
+    prec = pimc_gb300.PIMC_PREC_MIXED if args.precision == "mixed" else pimc_gb300.PIMC_PREC_FP64
+    kw0 = WL.serve_stream(1)[0][1]
+    base, _ = pimc_gb300.coulomb_tables(dict(kw0, counts=[2, 2], node_kind=[1, 1],
+                                             node_omega=[1.0, 1.0], sho_omega=[1.0, 1.0]))
+    seed = 20261203 + 1000003 * rank
+    pool = int(args.pool_gb * (1 << 30))
+    srv = pimc_gb300.Server(args.slots, pool, 64, 2048, 5, 32, seed=seed, precision=prec)
+    stream = torch.cuda.current_stream()
+    srv.set_stream(stream.cuda_stream)
+    # warm-up: a short stream served all at once (untimed)
+    warm = serve_requests(args, base, max(8, args.warmup * 8), seed=99)
+    budget = args.round_budget * serving.DEFAULT_ROUND_BUDGET
+    serving.ServeLoop(srv, round_budget=budget).run(warm, realtime=False)
+    reqs = serve_requests(args, base, args.requests, seed=WL.DEFAULT_SEED + rank)
+    loop = serving.ServeLoop(srv, round_budget=budget)
+    n_launch0 = srv.kernel_launches()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler() as clk:
+        t0 = time.perf_counter()
+        loop.run(reqs, realtime=True)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([wall], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        wall = float(t.item())
+    summ = serving.summary(reqs, wall)
+    beads = summ["bead_updates"]
+    offered = sum(r.beads for r in reqs) / max(reqs[-1].arrival, 1e-9)
+    h2d = sum(r.path.nbytes for r in reqs)
+    value = world * beads / wall
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": loop.rounds,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, loop.rounds),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded Poisson stream, seeded initial paths; Philox4x32-10 "
+                "proposals)",
+        "config": {"workload": "serve: " + describe("serve"),
+                   "step": "one serving round: every admitted simulation advances its own "
+                           "attempts (about equal device time each; 8 for N=64 at level 5), "
+                           "then its energy is measured",
+                   "requests": args.requests, "rate_per_s": args.rate,
+                   "sweep_scale": args.sweep_scale, "slots": args.slots,
+                   "pool_bytes": pool, "precision": args.precision,
+                   "offered_bead_updates_per_s": offered,
+                   "l2": "request paths and Slater caches (GBs in total) exceed L2",
+                   "parallelism": f"replicas{world}"},
+        "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"],
+                    "unit": "s, arrival to result"},
+        "e2e": {"value": value, "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d / max(1, loop.rounds)),
+                "d2h_bytes_per_step": int(args.slots * 8),
+                "path": "pimc_server_admit (host path) + pimc_server_run + pimc_server_energy "
+                        "per round + pimc_server_release"},
+        "gpu_launches": int(srv.kernel_launches() - n_launch0),
+        "gpu_busy_fraction": loop.busy / wall,
+        "admitted_while_others_ran": loop.overlapped,
+        "roofline": None,
+        "clocks": clk.summary(),
+    }
+    return out
+
+
 # ---------------------------------------------------------------- engine arm
 def run_engine(args, rank, world):
     import torch
     import pimc_gb300
+    if args.workload == "serve":
+        return run_serve(args, rank, world)
 
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
-    kw = workload_kw(args.workload)
+    kws = workload_kw(args.workload)
+    batch = isinstance(kws, list)
     R0, A0 = defaults(args.workload)
-    R = args.replicas or R0
+    R = len(kws) if batch else (args.replicas or R0)
+    kw = kws[0] if batch else kws
     A = args.attempts or A0 or sweep_attempts(kw)
-    L = kw["nlevel"]
     prec = pimc_gb300.PIMC_PREC_MIXED if args.precision == "mixed" else pimc_gb300.PIMC_PREC_FP64
-    tabs, ew = pimc_gb300.coulomb_tables(kw)
-    eng = pimc_gb300.Engine(kw, R, tabs, ew, seed=20261203 + 1000003 * rank, precision=prec)
+    seed = 20261203 + 1000003 * rank
+    if batch:
+        base, _ = pimc_gb300.coulomb_tables(dict(kw, counts=[2, 2], node_kind=[1, 1],
+                                                 node_omega=[1.0, 1.0], sho_omega=[1.0, 1.0]))
+        eng = pimc_gb300.Engine.batch(kws, [WL.tables_for(k, base) for k in kws], seed=seed,
+                                      precision=prec)
+        systems = kws
+    else:
+        tabs, ew = pimc_gb300.coulomb_tables(kw)
+        eng = pimc_gb300.Engine(kw, R, tabs, ew, seed=seed, precision=prec)
+        systems = [kw] * R
+    L = kw["nlevel"]
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
-    cfg_shape = (kw["nslice"], sum(kw["counts"]), 3)
 
-    class _C:
-        nslice, npart, cell = kw["nslice"], sum(kw["counts"]), [kw.get("cell", 1000.0)] * 3
+    def shape_of(k):
+        class _C:
+            nslice, npart, cell = k["nslice"], sum(k["counts"]), [k.get("cell", 1000.0)] * 3
+        return _C
 
-    paths = np.concatenate([WL.initial_path(_C, init_kind(args.workload), seed=100 + r).ravel()
-                            for r in range(R)])
+    paths = np.concatenate([WL.initial_path(shape_of(systems[r]), init_kind(args.workload),
+                                            seed=100 + r).ravel() for r in range(R)])
     host = torch.from_numpy(paths).pin_memory()
     eng.upload_paths(paths)
+    # launch configuration chosen by the autotuner (untimed; the chains are restored)
+    tuned, tried = eng.autotune(min(A, 16)) if not args.no_autotune else (eng.launch_config(), [])
     # depth statistics for the flop model (untimed)
     rec = eng.run_sections(4, records=True)
-    rl = rec["reject_level"].ravel()
-    reach = [float(np.mean((rl < 0) | (rl <= lev))) for lev in range(L + 1)]
+    # fraction of attempts that evaluate each level, by depth below the top level
+    Ls = np.array([k["nlevel"] for k in systems])[:, None]
+    rl = rec["reject_level"]
+    depth_reach = [float(np.mean((rl < 0) | (rl <= Ls - d))) for d in range(int(Ls.max()) + 1)]
+    reach = [depth_reach[L - lev] for lev in range(L + 1)]
     eng.upload_paths(paths)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
-        eng.run_sections(A)
-        energy = eng.thermo_energy()
+        eng.run_steps(A, 1, energies=False)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -255,18 +388,18 @@ def run_engine(args, rank, world):
         for i in range(args.steps):
             flush.fill_(float(i))
             ev[i][0].record(stream)
-            eng.run_sections(A)
-            energy = eng.thermo_energy()
+            eng.run_steps(A, 1, energies=False)  # one captured graph: sweep + measurement
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     launches = eng.kernel_launches - n_launch0
+    energy = eng.thermo_energy()  # energies after the last step (untimed re-measurement)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_ms = sum(step_ms)
     if world > 1:
         t = torch.tensor([t_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_ms = float(t.item())
-    units = R * A * ((1 << L) - 1)
+    units = A * sum((1 << k["nlevel"]) - 1 for k in systems)
     value = world * units * args.steps / (t_ms * 1e-3)
     # ---- end to end through the public API, host buffers each step
     e2e_steps = max(2, min(args.steps, 5))
@@ -275,13 +408,54 @@ def run_engine(args, rank, world):
     for _ in range(e2e_steps):
         eng.upload_paths(host.numpy())
         eng.run_sections(A)
-        energy = eng.thermo_energy()
+        e2e_energy = eng.thermo_energy()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * units * e2e_steps / e2e_s
+    # ---- energy against the FP64 form (same seeds, paths and step count)
+    assert np.all(np.isfinite(e2e_energy))
+    energy_block = energy_stats(energy)
+    if args.precision == "mixed":
+        if batch:
+            ref = pimc_gb300.Engine.batch(kws, [WL.tables_for(k, base) for k in kws], seed=seed)
+        else:
+            ref = pimc_gb300.Engine(kw, R, tabs, ew, seed=seed)
+        ref.set_stream(stream.cuda_stream)
+        ref.configure(tuned["block"], tuned["scratch_global"], tuned["ctas_per_sm"])
+        ref.upload_paths(paths)          # the same history as the measured engine:
+        ref.run_sections(4)              # depth-statistics attempts, re-upload,
+        ref.upload_paths(paths)          # warm-up and timed steps
+        for _ in range(args.warmup + args.steps):
+            ref.run_steps(A, 1, energies=False)
+        e64 = energy_stats(ref.thermo_energy())
+        ref.close()
+        energy_block["fp64"] = e64
+        diff = energy_block["value"] - e64["value"]
+        energy_block["diff_vs_fp64"] = diff
+        energy_block["diff_over_fp64_sigma"] = diff / e64["stat_err"] if e64["stat_err"] else None
+        energy_block["within_2sigma_of_fp64"] = bool(abs(diff) <= 2 * e64["stat_err"])
+    # ---- the plain form: one replica, FP64, same sweep (untimed by the step loop)
+    plain = None if batch else pimc_gb300.Engine(kw, 1, tabs, ew, seed=seed)
+    plain_value = None
+    if plain is not None:
+        plain.set_stream(stream.cuda_stream)
+        plain.upload_paths([paths[:3 * kw["nslice"] * sum(kw["counts"])]])
+        plain.run_steps(A, 1, energies=False)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(stream)
+        plain.run_steps(A, 1, energies=False)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        plain_value = A * ((1 << L) - 1) / (a0.elapsed_time(a1) * 1e-3)
+        plain.close()
     # ---- roofline of the dominant kernel (the section-move kernel)
     fp64_peak = pimc_gb300.fp64_peak_tflops()
-    flops = attempt_flops(kw, reach) * R * A
+    if batch:
+        flops = sum(attempt_flops(k, [depth_reach[k["nlevel"] - lev]
+                                      for lev in range(k["nlevel"] + 1)]) for k in systems) * A
+    else:
+        flops = attempt_flops(kw, reach) * R * A
     achieved = flops / (t_ms / args.steps * 1e-3) / 1e12
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -293,10 +467,12 @@ def run_engine(args, rank, world):
                    "step": "one sweep of section moves per replica + one thermodynamic "
                            "energy measurement per replica",
                    "replicas_per_gpu": R, "attempts_per_replica_per_step": A,
-                   "bead_updates_per_attempt": (1 << L) - 1, "precision": args.precision,
+                   "bead_updates_per_attempt": (1 << L) - 1 if not batch else "2^L-1 per replica",
+                   "precision": args.precision,
                    "l2": "paths (%.0f MB) exceed L2 and a 256 MB buffer is written between steps"
                          % (paths.nbytes / 1e6),
-                   "parallelism": f"replicas{world}"},
+                   "parallelism": f"replicas{world}",
+                   "launch": {"chosen": tuned, "candidates": tried}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(paths.nbytes),
                 "d2h_bytes_per_step": int(R * 8),
                 "path": "pimc_upload_paths (pinned host) + pimc_run_sections + pimc_thermo_energy"},
@@ -309,15 +485,39 @@ def run_engine(args, rank, world):
                      "flops_per_attempt_model": attempt_flops(kw, reach),
                      "level_reach": reach},
         "clocks": clk.summary(),
-        "energy_mean": float(np.mean(energy)),
+        "energy": energy_block,
     }
+    if plain_value is not None:
+        out["plain_fp64_single_replica"] = {
+            "value": plain_value, "unit": UNIT,
+            "what": "the same step on one replica in FP64 (pimc_run_steps, CUDA events)"}
+        out["batched_over_plain"] = value / plain_value
     return out
+
+
+def energy_stats(e):
+    """Mean thermodynamic energy over replicas and its standard error (replicas
+    are independent chains)."""
+    e = np.asarray(e, float)
+    ok = np.isfinite(e)
+    v = e[ok]
+    err = float(v.std(ddof=1) / math.sqrt(len(v))) if len(v) > 1 else None
+    return {"value": float(v.mean()) if len(v) else None, "stat_err": err,
+            "replicas": int(ok.sum()), "unit": "Hartree (reduced units)",
+            "when": "after the warm-up and timed steps"}
 
 
 def describe(name):
     return {
+        "batch4096": "4096 harmonic-dot replicas, N uniform 2..32 (SHONodes per spin, node "
+                     "temperature omega/4), omega uniform [0.5,2], M in {128,256,512,1024}, "
+                     "beta=M/25.6, level 4 or 5, Coulomb pair action norder 3",
         "dot20_fn": "3-D harmonic dot, N=20 (10 up, 10 down), SHONodes fixed node, beta=20, "
                     "M=1024, level 5, Coulomb pair action norder 3",
+        "serve": "Poisson stream of harmonic-dot simulations, N uniform 2..64 (SHONodes per "
+                 "spin, node temperature omega/4), omega uniform [0.5,2], M uniform in "
+                 "{64..2048} (powers of 2), beta=M/25.6, level 4 (M<=128) or 5, Coulomb pair "
+                 "action norder 3, requested sweeps log-uniform 1e3..1e5 times sweep_scale",
         "dot2": "3-D harmonic dot, N=2 (1 up, 1 down), beta=10, M=256, level 4, Coulomb "
                 "pair action norder 3",
         "heg54": "electron gas, N=54, r_s=4, T/T_F=0.5, Ewald |k|<5(2pi/L), "
@@ -327,6 +527,7 @@ def describe(name):
 
 def main():
     args = parse()
+    args.precision = workload_precision(args.workload, args.precision)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
@@ -337,7 +538,8 @@ def main():
             kw = workload_kw(args.workload)
             cores = os.cpu_count() or 1
             t0 = time.perf_counter()
-            value, attempts = cpu_throughput(kw, max(2.0, args.cpu_seconds / 2), cores)
+            value, attempts = cpu_throughput(kw, max(2.0, args.cpu_seconds / 2), cores,
+                                             defaults(args.workload)[1])
             wall = time.perf_counter() - t0
             kind = cpu_kind()
             out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
@@ -357,7 +559,7 @@ def main():
         if not args.no_cpu_baseline:
             kw = workload_kw(args.workload)
             cores = os.cpu_count() or 1
-            v, att = cpu_throughput(kw, args.cpu_seconds, cores)
+            v, att = cpu_throughput(kw, args.cpu_seconds, cores, defaults(args.workload)[1])
             out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": cpu_kind(),
                                    "sample": f"{att} section attempts of the same workload "
                                              f"over {cores} processes ({args.cpu_seconds:.0f} s)"}

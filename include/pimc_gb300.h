@@ -170,6 +170,78 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records);
 int pimc_replica_status(pimc_engine* e, int64_t* accepted, int64_t* attempted,
                         uint32_t* status);
 
+/* Runs nsteps steps, each nattempt section attempts on every replica followed by
+ * one energy measurement of every replica, as one CUDA graph (captured on the
+ * first call with these arguments, replayed afterwards).  host_energy, when not
+ * NULL, receives [nsteps][nreplica] energies and the call waits for them;
+ * otherwise it returns once the graph is enqueued.  This is pi-qmc's
+ * <Loop><ChooseSection/><Sample/><Measure/></Loop> body (src/parser/PIMCParser.cc)
+ * with the ThermoEnergyEstimator as the measurement. */
+int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy);
+
+/* ---- launch configuration and autotuning -------------------------------- */
+
+/* Launch configuration of an engine's section kernel: threads per replica
+ * (64, 128 or 256), the per-warp Slater scratch in shared (0) or global (1)
+ * memory, and the replicas resident per SM (0: as many as fit).  ms is the
+ * time the autotuner measured for it (0 when not measured).  A configuration
+ * changes how per-thread partial sums are grouped, so chains run under two
+ * configurations agree to rounding, not bit for bit. */
+typedef struct {
+  int block;
+  int scratch_global;
+  int ctas_per_sm;
+  float ms;
+} pimc_launch_config;
+
+int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg);
+int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg);
+/* Times each candidate configuration on nattempt section attempts per replica
+ * (paths, Slater caches and counters are restored after every trial, so tuning
+ * does not advance the chains), applies the fastest and returns it in *best;
+ * tried (up to max_tried entries, may be NULL) receives every candidate with
+ * its time and *ntried their number. */
+int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
+                         pimc_launch_config* tried, int max_tried, int* ntried);
+
+/* ---- serving ----------------------------------------------------------- */
+
+/* A server runs many independent simulations that come and go: each admitted
+ * simulation occupies a slot, its path and Slater-result cache live in one
+ * device pool of hbm_bytes, and every pimc_server_run advances all admitted
+ * slots in one persistent launch (continuous batching).  A simulation draws
+ * the random stream of its own stream_id, so its chain is the same whether it
+ * runs alone or among others.  The maxima fix the shared-memory layout. */
+typedef struct {
+  int slots;             /* concurrent simulations */
+  size_t hbm_bytes;      /* device pool for paths and caches */
+  int max_npart;
+  int max_nslice;
+  int max_level;
+  int max_node_count;    /* largest node-model species (0: no node models) */
+} pimc_server_config;
+
+int pimc_server_create(const pimc_server_config* cfg, uint64_t seed, int precision,
+                       pimc_engine** out);
+/* Admits one simulation (system, its pair tables, its initial path
+ * [nslice][npart][3]) that advances round_attempts section attempts in every
+ * round; *slot receives its slot.  Returns PIMC_ERR_CAPACITY
+ * when no slot is free or its path and cache do not fit the free pool (try
+ * again after a release), PIMC_ERR_INVALID when the system exceeds the
+ * server's maxima or needs Ewald sums. */
+int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_table* tables,
+                      int ntables, const double* host_path, uint32_t stream_id,
+                      int round_attempts, int* slot);
+int pimc_server_release(pimc_engine* e, int slot);
+/* One round: every admitted slot advances its round_attempts section-move
+ * attempts, all slots in one persistent launch (asynchronous). */
+int pimc_server_run(pimc_engine* e);
+/* Thermodynamic energy of every admitted slot (NaN for free slots). */
+int pimc_server_energy(pimc_engine* e, double* energy /* slots */);
+int pimc_server_download_path(pimc_engine* e, int slot, double* host_xyz);
+/* Bytes of the pool in use and free (largest free block). */
+int pimc_server_pool(pimc_engine* e, size_t* used, size_t* largest_free);
+
 /* ---- estimators -------------------------------------------------------- */
 
 /* Thermodynamic energy estimator of every replica's current path:
@@ -210,7 +282,7 @@ int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale);
  * latency-critical path.  No engine is needed and nothing is allocated: sys is
  * read by value, r1/r2 ([nbatch][npart][3]) and det/err ([nbatch]),
  * d1/d2 ([nbatch][npart]) are the caller's DEVICE buffers, the Slater-matrix
- * scratch is a fixed 3.1 MiB static device array (128 slots of 3136 doubles),
+ * scratch is a fixed 6.1 MiB static device array (128 slots of 6208 doubles),
  * and the kernel is issued on `stream` (cudaStream_t, NULL = legacy default).
  * scale is the node model's current scale (pimc_node_scale).  Limits: node
  * species of at most 32 particles, npart <= 1024; larger sizes return

@@ -54,6 +54,11 @@ struct DevBuf {
 
 }  // namespace
 
+// Layout choices the autotuner varies.
+struct LayoutOpts {
+  bool scratch_global = false;  // per-warp Slater scratch in global memory even when it fits
+};
+
 struct pimc_engine {
   int nrep = 0;
   int precision = PIMC_PREC_FP64;
@@ -73,12 +78,38 @@ struct pimc_engine {
   DevBuf<float> d_ugrid32;
   DevBuf<int> d_kvec;
   DevBuf<double> d_vk;
+  // serving: slots over one device pool
+  bool server = false;
+  pimc_server_config scfg{};
+  std::vector<char> active;
+  std::vector<long long> slot_path, slot_cache, slot_words;  // pool offsets / sizes (doubles)
+  std::map<long long, long long> free_blocks;                // offset -> size (doubles)
+  // pair tables on the device, found by content (host address first, then bytes)
+  std::multimap<const double*, std::pair<size_t, std::vector<double>>> table_dev;
+  size_t table_used = 0;
+  DevBuf<double> d_pool;
+  DevBuf<int> d_slot_attempts;  // attempts per round of each slot
+  std::vector<int> slot_attempts;
+  bool order_dirty = true;
+  int nactive = 0;
+  // energy measurement buffers and captured step graphs
+  DevBuf<double> d_partial;  // [nrep][kThermoChunks]
+  DevBuf<double> d_energy;   // [steps][nrep]
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_attempts = -1, graph_steps = -1;
   Layout lay{};
+  LayoutOpts lay_opts{};
+  int ctas_cap = 0;
   int block = kBlock;
   int grid = 0;
   int num_sms = 0;
   long long launches = 0;
   ~pimc_engine() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    d_partial.free();
+    d_energy.free();
     d_sys.free();
     d_state.free();
     d_paths.free();
@@ -86,6 +117,8 @@ struct pimc_engine {
     d_nodecache.free();
     d_order.free();
     d_next.free();
+    d_pool.free();
+    d_slot_attempts.free();
     d_ugrid.free();
     d_ugrid32.free();
     d_kvec.free();
@@ -177,6 +210,7 @@ void fill_sys(const pimc_system& s, DevSys& d) {
     }
   }
   d.tau = s.tau;
+  for (int i = 0; i < s.nspecies; ++i) d.node_dk[i] = std::sqrt(2 * s.spec_mass[i] / s.tau);
   for (int lev = 0; lev < kMaxLevels; ++lev) {
     const int nStride = 1 << lev;
     d.sho_div2[lev] = 1.0 / (2.0 * s.tau * nStride);
@@ -220,7 +254,17 @@ void fill_sys(const pimc_system& s, DevSys& d) {
   d.epsilon = s.epsilon > 0 ? s.epsilon : 1.0;
 }
 
-Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
+// Doubles of one Slater-result cache entry: epoch, determinant, two distance
+// vectors and the element matrix (SHO exp values; free-particle nodes add
+// three gradient matrices), rounded to an even count.
+int cache_entry_doubles(const DevSys& d) {
+  bool free_nodes = false;
+  for (int i = 0; i < d.nspecies; ++i) free_nodes |= d.node_kind[i] == PIMC_NODES_FREE;
+  const int n = d.ns_max;
+  return (2 + 2 * n + n * n * (free_nodes ? 4 : 1) + 1) & ~1;
+}
+
+Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutOpts opts = {}) {
   int nsec = 0, np = 0, nsm = 1, ewt = 0;
   bool fixed = false;
   for (const DevSys& d : sys) {
@@ -254,17 +298,28 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
     for (int i = 0; i < d.nspecies; ++i) sho |= d.node_kind[i] == PIMC_NODES_SHO;
   // exp-matrix cache of the moving species' section slices; left out (the
   // levels then recompute whole matrices) when it would not fit
-  L.ecache = (sho && (off + nsec * nsm * nsm) * 8 <= 120 * 1024) ? take(nsec * nsm * nsm) : -1;
-  L.ncol = fixed ? take(nsec * nsm) : -1;
+  // (only systems without the path-resident cache use it)
+  bool uncached = false;
+  for (const DevSys& d : sys) uncached |= d.fixed_node && !((1 << d.nlevel) < d.nslice / 2);
+  L.ecache = (sho && uncached && (off + nsec * nsm * nsm) * 8 <= 120 * 1024)
+                 ? take(nsec * nsm * nsm) : -1;
+  bool anyfree_col = false;
+  for (const DevSys& d : sys)
+    for (int i = 0; i < d.nspecies; ++i) anyfree_col |= d.node_kind[i] == PIMC_NODES_FREE;
+  L.ncol_stride = nsm * (anyfree_col ? 4 : 1);
+  L.ncol = fixed ? take(nsec * L.ncol_stride) : -1;
   // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n) doubles
   int stride = 0;
+  bool anyfree = false;
+  for (const DevSys& d : sys)
+    for (int i = 0; i < d.nspecies; ++i) anyfree |= d.node_kind[i] == PIMC_NODES_FREE;
   if (fixed)
     for (int n = 1; n <= nsm; ++n)
-      stride = std::max(stride, (32 / node_group_width(n)) * node_group_scratch(n));
+      stride = std::max(stride, (32 / node_group_width(n)) * node_group_scratch(n, anyfree));
   L.nodescr_stride = (stride + 1) & ~1;
   const int need = off + nwarps * L.nodescr_stride;
   const int limit = 200 * 1024 / 8;
-  if (need <= limit) {
+  if (need <= limit && !(opts.scratch_global && fixed)) {
     L.nodescr = take(nwarps * L.nodescr_stride);
     L.nodescr_in_smem = 1;
   } else {
@@ -274,6 +329,14 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok) {
   L.total = off;
   ok = L.total <= limit;
   return L;
+}
+
+void set_smem_caps() {
+  cudaFuncSetAttribute(section_moves_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
+  cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
 }
 
 int device_check(int& nsm) {
@@ -374,6 +437,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
         d.deltak[a] = 2 * 3.14159265358979 * d.cellb[a];
       }
     }
+    d.stream_id = (uint32_t)r;
     d.path_offset = off;
     e->path_off[r] = off;
     off += 3LL * s.nslice * s.npart;
@@ -426,13 +490,10 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
       }
     }
   }
-  // launch geometry: persistent grid over replicas
-  cudaFuncSetAttribute(section_moves_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       e->lay.total * 8);
-  cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       e->lay.total * 8);
-  cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       e->lay.total * 8);
+  // launch geometry: persistent grid over replicas.  The dynamic shared-memory
+  // cap is the layout limit for every engine (the attribute is per function,
+  // shared by all engines of the process).
+  set_smem_caps();
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, e->block,
                                                 e->lay.total * 8);
@@ -453,7 +514,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
     long long coff = 0;
     for (DevSys& d : e->hsys) {
       const bool use = d.fixed_node && (1 << d.nlevel) < d.nslice / 2;
-      d.nc_stride = (2 + 2 * d.ns_max + d.ns_max * d.ns_max + 1) & ~1;
+      d.nc_stride = cache_entry_doubles(d);
       if (use) {
         d.nc_offset = coff;
         coff += (long long)d.nspecies * d.nslice * d.nc_stride;
@@ -565,6 +626,54 @@ int pimc_path_offsets(pimc_engine* e, int64_t* offsets) {
   return PIMC_OK;
 }
 
+namespace {
+constexpr int kThermoChunks = 64;
+
+// Enqueues the energy measurement of every replica into d_energy[row][*].
+int enqueue_thermo(pimc_engine* e, cudaStream_t st, int row) {
+  if (e->d_partial.n < (size_t)e->nrep * kThermoChunks &&
+      e->d_partial.alloc((size_t)e->nrep * kThermoChunks))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc energy partials");
+  if (e->d_energy.n < (size_t)(row + 1) * e->nrep) {
+    DevBuf<double> bigger;
+    if (bigger.alloc((size_t)(row + 1) * e->nrep)) return fail(PIMC_ERR_CUDA, "cudaMalloc energies");
+    std::swap(bigger.p, e->d_energy.p);
+    std::swap(bigger.n, e->d_energy.n);
+  }
+  ThermoParams P;
+  P.sys = e->d_sys.p;
+  P.index = nullptr;
+  P.paths = e->d_paths.p;
+  P.partial = e->d_partial.p;
+  P.nchunk = kThermoChunks;
+  P.nrep = e->nrep;
+  P.lay = e->lay;
+  thermo_kernel<<<dim3(kThermoChunks, e->nrep), kBlock, e->lay.total * 8, st>>>(P);
+  thermo_reduce_kernel<<<(e->nrep + 127) / 128, 128, 0, st>>>(
+      e->d_sys.p, nullptr, e->d_partial.p, kThermoChunks, e->nrep,
+      e->d_energy.p + (size_t)row * e->nrep);
+  e->launches += 2;
+  CU(cudaGetLastError());
+  return PIMC_OK;
+}
+
+void fill_run_params(pimc_engine* e, RunParams& P, int nattempt, pimc_move_record* d_rec) {
+  P.sys = e->d_sys.p;
+  P.state = e->d_state.p;
+  P.paths = e->d_paths.p;
+  P.nodescr_g = e->d_nodescr.p;
+  P.nodecache = e->d_nodecache.p;
+  P.rec = d_rec;
+  P.order = e->d_order.p;
+  P.next = e->d_next.p;
+  P.nattempt = nattempt;
+  P.nattempt_r = nullptr;
+  P.nrep = e->nrep;
+  P.seed = e->seed;
+  P.lay = e->lay;
+}
+}  // namespace
+
 int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
   if (!e || nattempt < 0) return fail(PIMC_ERR_INVALID, "bad argument");
   if (nattempt == 0) return PIMC_OK;
@@ -574,19 +683,8 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
     CU(cudaMemsetAsync(d_rec, 0, sizeof(pimc_move_record) * (size_t)e->nrep * nattempt, e->stream));
   }
   RunParams P;
-  P.sys = e->d_sys.p;
-  P.state = e->d_state.p;
-  P.paths = e->d_paths.p;
-  P.nodescr_g = e->d_nodescr.p;
-  P.nodecache = e->d_nodecache.p;
-  P.rec = d_rec;
-  P.order = e->d_order.p;
-  P.next = e->d_next.p;
+  fill_run_params(e, P, nattempt, d_rec);
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  P.nattempt = nattempt;
-  P.nrep = e->nrep;
-  P.seed = e->seed;
-  P.lay = e->lay;
   section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
@@ -624,31 +722,67 @@ int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale) {
   return PIMC_OK;
 }
 
+
 int pimc_thermo_energy(pimc_engine* e, double* host_energy) {
   if (!e || !host_energy) return fail(PIMC_ERR_INVALID, "null argument");
-  int maxm = 0;
-  for (const DevSys& d : e->hsys) maxm = std::max(maxm, d.nslice);
-  const int nchunk = std::max(1, std::min(64, maxm / 8));
-  double* d_part = nullptr;
-  CU(cudaMallocAsync(&d_part, sizeof(double) * (size_t)e->nrep * nchunk, e->stream));
-  ThermoParams P;
-  P.sys = e->d_sys.p;
-  P.paths = e->d_paths.p;
-  P.partial = d_part;
-  P.nchunk = nchunk;
-  P.nrep = e->nrep;
-  P.lay = e->lay;
-  thermo_kernel<<<dim3(nchunk, e->nrep), kBlock, e->lay.total * 8, e->stream>>>(P);
-  e->launches++;
-  CU(cudaGetLastError());
-  std::vector<double> part((size_t)e->nrep * nchunk);
-  CU(cudaMemcpyAsync(part.data(), d_part, part.size() * 8, cudaMemcpyDeviceToHost, e->stream));
-  CU(cudaFreeAsync(d_part, e->stream));
+  if (e->server) return fail(PIMC_ERR_INVALID, "use pimc_server_energy on a server");
+  if (int rc = enqueue_thermo(e, e->stream, 0)) return rc;
+  CU(cudaMemcpyAsync(host_energy, e->d_energy.p, e->nrep * sizeof(double),
+                     cudaMemcpyDeviceToHost, e->stream));
   CU(cudaStreamSynchronize(e->stream));
-  for (int r = 0; r < e->nrep; ++r) {
-    double s = 0;
-    for (int c = 0; c < nchunk; ++c) s += part[(size_t)r * nchunk + c];
-    host_energy[r] = s / e->hsys[r].nslice;
+  return PIMC_OK;
+}
+
+int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy) {
+  if (!e || e->server || nattempt < 0 || nsteps <= 0)
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  if (e->graph && (e->graph_attempts != nattempt || e->graph_steps != nsteps)) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  if (!e->graph) {
+    // make the buffers the graph will use before capturing it
+    if (e->d_partial.n < (size_t)e->nrep * kThermoChunks &&
+        e->d_partial.alloc((size_t)e->nrep * kThermoChunks))
+      return fail(PIMC_ERR_CUDA, "cudaMalloc energy partials");
+    if (e->d_energy.n < (size_t)nsteps * e->nrep && e->d_energy.alloc((size_t)nsteps * e->nrep))
+      return fail(PIMC_ERR_CUDA, "cudaMalloc energies");
+    if (!e->cap_stream) CU(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking));
+    const long long l0 = e->launches;
+    CU(cudaStreamBeginCapture(e->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PIMC_OK;
+    for (int k = 0; k < nsteps && rc == PIMC_OK; ++k) {
+      if (nattempt > 0) {
+        RunParams P;
+        fill_run_params(e, P, nattempt, nullptr);
+        cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->cap_stream);
+        section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->cap_stream>>>(P);
+      }
+      rc = enqueue_thermo(e, e->cap_stream, k);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->cap_stream, &g);
+    e->launches = l0;
+    if (rc != PIMC_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(PIMC_ERR_CUDA, cudaGetErrorString(ce));
+    const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      e->graph = nullptr;
+      return fail(PIMC_ERR_CUDA, cudaGetErrorString(ie));
+    }
+    e->graph_attempts = nattempt;
+    e->graph_steps = nsteps;
+  }
+  CU(cudaGraphLaunch(e->graph, e->stream));
+  e->launches += (long long)nsteps * ((nattempt > 0 ? 1 : 0) + 2);
+  if (host_energy) {
+    CU(cudaMemcpyAsync(host_energy, e->d_energy.p, (size_t)nsteps * e->nrep * sizeof(double),
+                       cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
   }
   return PIMC_OK;
 }
@@ -780,6 +914,458 @@ int pimc_fp64_peak(double* tflops) {
 }
 
 int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
+
+// ------------------------------------------------- launch configuration
+namespace {
+int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap) {
+  if (block != 64 && block != 128 && block != 256) return fail(PIMC_ERR_INVALID, "block must be 64, 128 or 256");
+  bool ok = false;
+  const Layout L = make_layout(e->hsys, block / 32, ok, opts);
+  if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
+  int occ = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, block, L.total * 8);
+  occ = std::max(occ, 1);
+  if (ctas_cap > 0) occ = std::min(occ, ctas_cap);
+  const int grid = std::min(e->nrep, e->num_sms * occ);
+  if (!L.nodescr_in_smem) {
+    const size_t need = (size_t)grid * (block / 32) * L.nodescr_stride;
+    if (need > e->d_nodescr.n) {
+      CU(cudaStreamSynchronize(e->stream));
+      if (e->d_nodescr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
+    }
+  }
+  e->lay = L;
+  e->lay_opts = opts;
+  e->ctas_cap = ctas_cap;
+  e->block = block;
+  e->grid = grid;
+  if (e->graph) {  // captured with the old launch shape
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return PIMC_OK;
+}
+}  // namespace
+
+int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg) {
+  if (!e || e->server || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
+  LayoutOpts o;
+  o.scratch_global = cfg->scratch_global != 0;
+  return apply_config(e, cfg->block, o, cfg->ctas_per_sm);
+}
+
+int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg) {
+  if (!e || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
+  cfg->block = e->block;
+  cfg->scratch_global = e->lay.nodescr_in_smem ? 0 : 1;
+  cfg->ctas_per_sm = e->ctas_cap;
+  cfg->ms = 0.f;
+  return PIMC_OK;
+}
+
+int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
+                         pimc_launch_config* tried, int max_tried, int* ntried) {
+  if (!e || e->server || nattempt <= 0 || !best) return fail(PIMC_ERR_INVALID, "bad argument");
+  // state the trials advance, kept aside and restored before each trial
+  DevBuf<double> paths0, cache0;
+  DevBuf<DevState> state0;
+  const size_t np_ = e->path_off[e->nrep];
+  if (paths0.alloc(np_) || state0.alloc(e->nrep) || cache0.alloc(e->d_nodecache.n))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc autotune backup");
+  auto copy = [&](bool save) -> int {
+    CU(cudaMemcpyAsync(save ? paths0.p : e->d_paths.p, save ? e->d_paths.p : paths0.p,
+                       np_ * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+    CU(cudaMemcpyAsync(save ? state0.p : e->d_state.p, save ? e->d_state.p : state0.p,
+                       e->nrep * sizeof(DevState), cudaMemcpyDeviceToDevice, e->stream));
+    if (e->d_nodecache.n)
+      CU(cudaMemcpyAsync(save ? cache0.p : e->d_nodecache.p, save ? e->d_nodecache.p : cache0.p,
+                         e->d_nodecache.n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+    return PIMC_OK;
+  };
+  if (int rc = copy(true)) return rc;
+  const long long launches0 = e->launches;
+  const int blk0 = e->block, cap0 = e->ctas_cap;
+  const LayoutOpts opt0 = e->lay_opts;
+  bool fixed = false;
+  for (const DevSys& d : e->hsys) fixed |= d.fixed_node != 0;
+  std::vector<pimc_launch_config> cand;
+  for (int b : {64, 128, 256})
+    for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({b, g, 0, 0.f});
+  cudaEvent_t t0, t1;
+  CU(cudaEventCreate(&t0));
+  CU(cudaEventCreate(&t1));
+  int nt = 0, ibest = -1;
+  for (pimc_launch_config& c : cand) {
+    LayoutOpts o;
+    o.scratch_global = c.scratch_global != 0;
+    if (apply_config(e, c.block, o, c.ctas_per_sm) != PIMC_OK) {
+      c.ms = -1.f;  // does not fit
+      continue;
+    }
+    float best_ms = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {  // a warm-up trial, then the timed one
+      if (int rc = copy(false)) return rc;
+      CU(cudaEventRecord(t0, e->stream));
+      if (int rc = pimc_run_sections(e, nattempt, nullptr)) return rc;
+      CU(cudaEventRecord(t1, e->stream));
+      CU(cudaEventSynchronize(t1));
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, t0, t1));
+      if (rep == 1) best_ms = ms;
+    }
+    c.ms = best_ms;
+    if (ibest < 0 || c.ms < cand[ibest].ms) ibest = (int)(&c - &cand[0]);
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  for (const pimc_launch_config& c : cand) {
+    if (tried && nt < max_tried) tried[nt] = c;
+    ++nt;
+  }
+  if (ntried) *ntried = nt;
+  int rc;
+  if (ibest >= 0) {
+    LayoutOpts o;
+    o.scratch_global = cand[ibest].scratch_global != 0;
+    rc = apply_config(e, cand[ibest].block, o, cand[ibest].ctas_per_sm);
+    *best = cand[ibest];
+  } else {
+    rc = apply_config(e, blk0, opt0, cap0);
+    pimc_engine_get_config(e, best);
+  }
+  if (int rc2 = copy(false)) return rc2;
+  CU(cudaStreamSynchronize(e->stream));
+  e->launches = launches0;  // trials are not the caller's launches
+  return rc;
+}
+
+// ---------------------------------------------------------------- serving
+namespace {
+long long pool_alloc(pimc_engine* e, long long words) {
+  for (auto it = e->free_blocks.begin(); it != e->free_blocks.end(); ++it) {
+    if (it->second >= words) {
+      const long long off = it->first, rest = it->second - words;
+      e->free_blocks.erase(it);
+      if (rest > 0) e->free_blocks[off + words] = rest;
+      return off;
+    }
+  }
+  return -1;
+}
+void pool_free(pimc_engine* e, long long off, long long words) {
+  if (words <= 0) return;
+  auto it = e->free_blocks.emplace(off, words).first;
+  auto nx = std::next(it);
+  if (nx != e->free_blocks.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    e->free_blocks.erase(nx);
+  }
+  if (it != e->free_blocks.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      e->free_blocks.erase(it);
+    }
+  }
+}
+int refresh_order(pimc_engine* e) {
+  if (!e->order_dirty) return 0;
+  std::vector<std::pair<double, int>> act;
+  for (int r = 0; r < e->nrep; ++r)
+    if (e->active[r]) {
+      const DevSys& d = e->hsys[r];
+      double c = (double)d.npart * d.npart;
+      for (int i = 0; i < d.nspecies; ++i)
+        if (d.node_kind[i]) c += 2.0 * d.spec_count[i] * d.spec_count[i] * (d.spec_count[i] + 20);
+      act.push_back({-c * ((1 << d.nlevel) + 1), r});
+    }
+  std::stable_sort(act.begin(), act.end());
+  std::vector<int> order(act.size());
+  std::vector<DevSys> live;
+  for (size_t k = 0; k < act.size(); ++k) {
+    order[k] = act[k].second;
+    live.push_back(e->hsys[act[k].second]);
+  }
+  e->nactive = (int)order.size();
+  if (!order.empty()) {
+    // shared-memory layout and grid sized to the systems now admitted; the
+    // block size stays fixed so that a slot's arithmetic never depends on the mix
+    bool ok = false;
+    e->lay = make_layout(live, e->block / 32, ok);
+    if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, e->block,
+                                                  e->lay.total * 8);
+    e->grid = std::min(e->nactive, e->num_sms * std::max(occ, 1));
+    if (!e->lay.nodescr_in_smem) {
+      const size_t need = (size_t)e->grid * (e->block / 32) * e->lay.nodescr_stride;
+      if (need > e->d_nodescr.n) {
+        CU(cudaStreamSynchronize(e->stream));
+        if (e->d_nodescr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
+      }
+    }
+    CU(cudaMemcpyAsync(e->d_order.p, order.data(), order.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+  }
+  e->order_dirty = false;
+  return 0;
+}
+}  // namespace
+
+int pimc_server_create(const pimc_server_config* cfg, uint64_t seed, int precision,
+                       pimc_engine** out) {
+  if (!cfg || !out || cfg->slots <= 0 || cfg->hbm_bytes < 1024 || cfg->max_npart <= 0 ||
+      cfg->max_level < 1 || cfg->max_level > PIMC_MAX_LEVEL || cfg->max_nslice <= 0 ||
+      cfg->max_node_count < 0 || cfg->max_node_count > PIMC_MAX_NODE_PARTICLES)
+    return fail(PIMC_ERR_INVALID, "bad server configuration");
+  *out = nullptr;
+  int nsm = 0;
+  if (int rc = device_check(nsm)) return rc;
+  pimc_engine* e = new pimc_engine();
+  e->server = true;
+  e->scfg = *cfg;
+  e->nrep = cfg->slots;
+  e->seed = seed;
+  e->precision = precision;
+  e->num_sms = nsm;
+  e->hsys.assign(cfg->slots, DevSys());
+  e->hdesc.resize(cfg->slots);
+  e->active.assign(cfg->slots, 0);
+  e->slot_path.assign(cfg->slots, -1);
+  e->slot_cache.assign(cfg->slots, -1);
+  e->slot_words.assign(cfg->slots, 0);
+  e->slot_attempts.assign(cfg->slots, 1);
+  e->path_off.assign(cfg->slots + 1, 0);
+  // layout for the largest admissible system
+  DevSys mx;
+  memset(&mx, 0, sizeof(mx));
+  mx.npart = cfg->max_npart;
+  mx.nlevel = cfg->max_level;
+  mx.nsec = (1 << cfg->max_level) + 1;
+  mx.nslice = cfg->max_nslice;
+  mx.ns_max = std::max(1, cfg->max_node_count);
+  mx.fixed_node = cfg->max_node_count > 0;
+  mx.nspecies = 2;
+  mx.node_kind[0] = mx.fixed_node ? PIMC_NODES_SHO : 0;
+  std::vector<DevSys> one(1, mx);
+  e->block = kBlock;
+  bool ok = false;
+  const Layout biggest = make_layout(one, e->block / 32, ok);
+  if (!ok) {
+    delete e;
+    return fail(PIMC_ERR_CAPACITY, "largest system does not fit in shared memory");
+  }
+  set_smem_caps();
+  e->lay = biggest;
+  e->grid = std::min(cfg->slots, nsm);
+  const long long words = (long long)(cfg->hbm_bytes / sizeof(double));
+  if (e->d_pool.alloc(words) || e->d_sys.alloc(cfg->slots) || e->d_state.alloc(cfg->slots) ||
+      e->d_order.alloc(cfg->slots) || e->d_next.alloc(1) || e->d_slot_attempts.alloc(cfg->slots) || e->d_ugrid.alloc(1 << 22) ||
+      e->d_ugrid32.alloc(1 << 22)) {
+    delete e;
+    return fail(PIMC_ERR_CUDA, "cudaMalloc server pool");
+  }
+  e->free_blocks[0] = words;
+  *out = e;
+  return PIMC_OK;
+}
+
+int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_table* tables,
+                      int ntables, const double* host_path, uint32_t stream_id,
+                      int round_attempts, int* slot) {
+  if (!e || !e->server || !sys || !host_path || !slot || (ntables > 0 && !tables) ||
+      round_attempts <= 0)
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  if (int rc = validate(*sys)) return rc == PIMC_ERR_CAPACITY ? PIMC_ERR_INVALID : rc;
+  if (sys->ewald) return fail(PIMC_ERR_INVALID, "the server takes no Ewald systems");
+  DevSys d;
+  fill_sys(*sys, d);
+  if (d.npart > e->scfg.max_npart || d.nlevel > e->scfg.max_level ||
+      d.nslice > e->scfg.max_nslice || (d.fixed_node && d.ns_max > e->scfg.max_node_count))
+    return fail(PIMC_ERR_INVALID, "system larger than the server's maxima");
+  int r = -1;
+  for (int k = 0; k < e->nrep; ++k)
+    if (!e->active[k]) {
+      r = k;
+      break;
+    }
+  if (r < 0) return fail(PIMC_ERR_CAPACITY, "no free slot");
+  const long long pw = 3LL * sys->nslice * sys->npart;
+  const bool cache = d.fixed_node && (1 << d.nlevel) < d.nslice / 2;
+  d.nc_stride = cache_entry_doubles(d);
+  const long long cw = cache ? (long long)d.nspecies * d.nslice * d.nc_stride : 0;
+  const long long po = pool_alloc(e, pw + cw);
+  if (po < 0) return fail(PIMC_ERR_CAPACITY, "device pool full");
+  // pair tables: one device copy per distinct host table
+  if (sys->coulomb) {
+    if (ntables > kMaxTables) {
+      pool_free(e, po, pw + cw);
+      return fail(PIMC_ERR_CAPACITY, "too many pair tables");
+    }
+    for (int k = 0; k < ntables; ++k) {
+      const pimc_pair_table& t = tables[k];
+      if (t.species1 < 0 || t.species1 >= sys->nspecies || t.species2 < 0 ||
+          t.species2 >= sys->nspecies || t.ngpts < 2 || t.norder < 0 || !t.ugrid) {
+        pool_free(e, po, pw + cw);
+        return fail(PIMC_ERR_INVALID, "bad pair table");
+      }
+      const size_t words = (size_t)t.ngpts * 2 * (t.norder + 1);
+      size_t toff = (size_t)-1;
+      auto range = e->table_dev.equal_range(t.ugrid);
+      for (auto it = range.first; it != range.second; ++it)
+        if (it->second.second.size() == words &&
+            std::equal(t.ugrid, t.ugrid + words, it->second.second.begin()))
+          toff = it->second.first;
+      if (toff == (size_t)-1) {
+        if (e->table_used + words > e->d_ugrid.n) {
+          pool_free(e, po, pw + cw);
+          return fail(PIMC_ERR_INVALID, "server table pool full (distinct pair tables exceed 32 MiB)");
+        }
+        toff = e->table_used;
+        std::vector<float> f(t.ugrid, t.ugrid + words);
+        CU(cudaMemcpy(e->d_ugrid.p + toff, t.ugrid, words * 8, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(e->d_ugrid32.p + toff, f.data(), words * 4, cudaMemcpyHostToDevice));
+        e->table_used += words;
+        e->table_dev.emplace(t.ugrid, std::make_pair(toff, std::vector<double>(t.ugrid, t.ugrid + words)));
+      }
+      DevTable& dt = d.tab[k];
+      dt.ngpts = t.ngpts;
+      dt.norder = t.norder;
+      dt.ndata = t.norder + 1;
+      dt.s1 = t.species1;
+      dt.s2 = t.species2;
+      dt.ifirst1 = d.spec_first[t.species1];
+      dt.npart1 = d.spec_count[t.species1];
+      dt.ifirst2 = d.spec_first[t.species2];
+      dt.npart2 = d.spec_count[t.species2];
+      dt.rgridinv = t.rgridinv;
+      dt.logrratioinv = t.logrratioinv;
+      dt.ugrid = e->d_ugrid.p + toff;
+      dt.ugrid32 = e->d_ugrid32.p + toff;
+    }
+    d.ntab = ntables;
+  }
+  d.mixed = e->precision == PIMC_PREC_MIXED;
+  d.stream_id = stream_id;
+  d.path_offset = po;
+  d.nc_offset = cache ? po + pw : -1;
+  d.inv_offset = e->lay.nodescr_in_smem ? -1 : 0;
+  e->hsys[r] = d;
+  e->hdesc[r] = *sys;
+  e->slot_path[r] = po;
+  e->slot_words[r] = pw + cw;
+  e->active[r] = 1;
+  e->order_dirty = true;
+  DevState st;
+  memset(&st, 0, sizeof(st));
+  for (int k = 0; k < kMaxSpecies; ++k) st.node_scale[k] = 1.0;
+  CU(cudaMemcpyAsync(e->d_sys.p + r, &e->hsys[r], sizeof(DevSys), cudaMemcpyHostToDevice,
+                     e->stream));
+  CU(cudaMemcpyAsync(e->d_state.p + r, &st, sizeof(DevState), cudaMemcpyHostToDevice, e->stream));
+  e->slot_attempts[r] = round_attempts;
+  CU(cudaMemcpyAsync(e->d_slot_attempts.p + r, &e->slot_attempts[r], sizeof(int),
+                     cudaMemcpyHostToDevice, e->stream));
+  CU(cudaMemcpyAsync(e->d_pool.p + po, host_path, pw * sizeof(double), cudaMemcpyHostToDevice,
+                     e->stream));
+  if (cw) CU(cudaMemsetAsync(e->d_pool.p + po + pw, 0xff, cw * sizeof(double), e->stream));
+  CU(cudaStreamSynchronize(e->stream));  // the host copies above are from caller memory
+  *slot = r;
+  return PIMC_OK;
+}
+
+int pimc_server_release(pimc_engine* e, int slot) {
+  if (!e || !e->server || slot < 0 || slot >= e->nrep || !e->active[slot])
+    return fail(PIMC_ERR_INVALID, "bad slot");
+  CU(cudaStreamSynchronize(e->stream));  // no launch may still use the slot's memory
+  pool_free(e, e->slot_path[slot], e->slot_words[slot]);
+  e->active[slot] = 0;
+  e->order_dirty = true;
+  return PIMC_OK;
+}
+
+int pimc_server_run(pimc_engine* e) {
+  if (!e || !e->server) return fail(PIMC_ERR_INVALID, "bad argument");
+  if (int rc = refresh_order(e)) return rc;
+  if (e->nactive == 0) return PIMC_OK;
+  const int nattempt = 0;
+  RunParams P;
+  P.sys = e->d_sys.p;
+  P.state = e->d_state.p;
+  P.paths = e->d_pool.p;
+  P.nodescr_g = e->d_nodescr.p;
+  P.nodecache = e->d_pool.p;
+  P.rec = nullptr;
+  P.order = e->d_order.p;
+  P.next = e->d_next.p;
+  P.nattempt = nattempt;
+  P.nattempt_r = e->d_slot_attempts.p;
+  P.nrep = e->nactive;
+  P.seed = e->seed;
+  P.lay = e->lay;
+  CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
+  section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->stream>>>(P);
+  e->launches++;
+  CU(cudaGetLastError());
+  return PIMC_OK;
+}
+
+int pimc_server_energy(pimc_engine* e, double* energy) {
+  if (!e || !e->server || !energy) return fail(PIMC_ERR_INVALID, "bad argument");
+  if (int rc = refresh_order(e)) return rc;
+  for (int r = 0; r < e->nrep; ++r) energy[r] = std::nan("");
+  if (e->nactive == 0) return PIMC_OK;
+  // a fixed chunk count: each slot's sum is grouped the same way whatever the mix
+  const int nchunk = 64;
+  double* d_part = nullptr;
+  CU(cudaMallocAsync(&d_part, sizeof(double) * (size_t)e->nactive * nchunk, e->stream));
+  ThermoParams P;
+  P.sys = e->d_sys.p;
+  P.index = e->d_order.p;
+  P.paths = e->d_pool.p;
+  P.partial = d_part;
+  P.nchunk = nchunk;
+  P.nrep = e->nactive;
+  P.lay = e->lay;
+  thermo_kernel<<<dim3(nchunk, e->nactive), kBlock, e->lay.total * 8, e->stream>>>(P);
+  e->launches++;
+  CU(cudaGetLastError());
+  std::vector<double> part((size_t)e->nactive * nchunk);
+  std::vector<int> order(e->nactive);
+  CU(cudaMemcpyAsync(part.data(), d_part, part.size() * 8, cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaMemcpyAsync(order.data(), e->d_order.p, order.size() * 4, cudaMemcpyDeviceToHost,
+                     e->stream));
+  CU(cudaFreeAsync(d_part, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  for (int k = 0; k < e->nactive; ++k) {
+    double s = 0;
+    for (int c = 0; c < nchunk; ++c) s += part[(size_t)k * nchunk + c];
+    energy[order[k]] = s / e->hsys[order[k]].nslice;
+  }
+  return PIMC_OK;
+}
+
+int pimc_server_download_path(pimc_engine* e, int slot, double* host_xyz) {
+  if (!e || !e->server || slot < 0 || slot >= e->nrep || !e->active[slot] || !host_xyz)
+    return fail(PIMC_ERR_INVALID, "bad slot");
+  const long long pw = 3LL * e->hdesc[slot].nslice * e->hdesc[slot].npart;
+  CU(cudaMemcpyAsync(host_xyz, e->d_pool.p + e->slot_path[slot], pw * sizeof(double),
+                     cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return PIMC_OK;
+}
+
+int pimc_server_pool(pimc_engine* e, size_t* used, size_t* largest_free) {
+  if (!e || !e->server) return fail(PIMC_ERR_INVALID, "not a server");
+  long long fr = 0, big = 0;
+  for (auto& b : e->free_blocks) {
+    fr += b.second;
+    big = std::max(big, b.second);
+  }
+  if (used) *used = (size_t)(e->d_pool.n - fr) * sizeof(double);
+  if (largest_free) *largest_free = (size_t)big * sizeof(double);
+  return PIMC_OK;
+}
 
 // Allocation-free node evaluation.  The device address of the static scratch
 // array is looked up once per device (cudaGetSymbolAddress, with that device

@@ -10,6 +10,7 @@ namespace pimc {
 // for the largest replica of a launch.
 struct Layout {
   int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
+  int ncol_stride;
   int nodescr_in_smem;
   int nodescr_stride;
   int total;  // doubles
@@ -25,6 +26,7 @@ struct RunParams {
   const int* order;  // replicas in decreasing cost (longest first)
   int* next;         // work-queue head, zeroed before each launch
   int nattempt;
+  const int* nattempt_r;  // per-replica attempts (null: nattempt for every replica)
   int nrep;
   uint64_t seed;
   Layout lay;
@@ -54,6 +56,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.ictl = (int*)(base + L.ictl);
   m.ecache = L.ecache >= 0 ? base + L.ecache : nullptr;
   m.ncol = L.ncol >= 0 ? base + L.ncol : nullptr;
+  m.ncol_stride = L.ncol_stride;
   m.nodescr_stride = L.nodescr_stride;
   m.nodescr = L.nodescr_in_smem
                   ? base + L.nodescr
@@ -240,8 +243,8 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
     if (!s.node_kind[sp]) continue;
     const int n = s.spec_count[sp];
     const int W = node_group_width(n), G = 32 / W, g = lane / W, gl = lane & (W - 1);
-    double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
     const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
+    double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
     const bool mine = sp == msp;
     int start = 0;
     for (int round = 0; round < 64; ++round) {
@@ -275,8 +278,8 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
         SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
         double det = 0;
         int err = 0;
-        double* ec = sho ? (e ? e + 2 + 2 * n : (mine ? m.ecache + (size_t)t * n * n : nullptr))
-                         : nullptr;
+        double* ec = e ? e + 2 + 2 * n
+                       : ((sho && mine && m.ecache) ? m.ecache + (size_t)t * n * n : nullptr);
         // with a cache every miss is evaluated in full so that its entry is complete
         const int full = (mine || e) ? 1 : 0;
         double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
@@ -319,7 +322,7 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
         int err = errs[k];
         double sc2 = scale[sp];
         int guard = 0;
-        double* dsc = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
+        double* dsc = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
         while (err || fabs(det) < 1e-50 || fabs(det) > 1e50) {
           if (err || ++guard > 2000) {
             if (lane == 0) *status |= err ? (PIMC_STATUS_SINGULAR | PIMC_STATUS_RESCALE_LIMIT)
@@ -379,8 +382,8 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
   const int nStride = 1 << (level + 1);
   const int n = s.spec_count[msp];
   const int W = node_group_width(n), G = 32 / W, g = lane / W;
-  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n);
   const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
+  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
   const int jcol = ipart - s.spec_first[msp];
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
@@ -394,15 +397,13 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
     double det = 0;
     int err = 0;
     double* ec = nullptr;
-    if (sho) {
-      if (cache)
-        ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
-      else if (m.ecache)
-        ec = m.ecache + (size_t)t * n * n;
-    }
+    if (cache)
+      ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
+    else if (sho && m.ecache)
+      ec = m.ecache + (size_t)t * n * n;
     node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
                        m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                       (sho && cache) ? m.ncol + t * nsm : nullptr);
+                       cache ? m.ncol + t * m.ncol_stride : nullptr);
     if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
@@ -418,6 +419,16 @@ __device__ double node_level(const DevSys& s, const Smem& m, double scale, int m
     const double* Dp0 = m.dist + ((t - 1) * 2) * nsm;
     const double* N0 = m.ndist + (t * 2) * nsm;
     const double* Np0 = m.ndist + ((t - 1) * 2) * nsm;
+    if (s.mixed) {
+      // FP32 terms (1 - e^-x through expm1 keeps them accurate near the node),
+      // summed in FP64
+      const float a1 = -expm1f(-(float)(D0[p] * Dp0[p]));
+      const float b1 = -expm1f(-(float)(N0[p] * Np0[p]));
+      const float a2 = -expm1f(-(float)(D0[nsm + p] * Dp0[nsm + p]));
+      const float b2 = -expm1f(-(float)(N0[nsm + p] * Np0[nsm + p]));
+      part += (double)(logf(a1) - logf(b1)) + (double)(logf(a2) - logf(b2));
+      continue;
+    }
     double a = log((1 - exp(-D0[p] * Dp0[p])) / (1 - exp(-N0[p] * Np0[p])));
     a += log((1 - exp(-D0[nsm + p] * Dp0[nsm + p])) / (1 - exp(-N0[nsm + p] * Np0[nsm + p])));
     part += a;
@@ -477,13 +488,14 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
     double* cache = (P.nodecache && s.nc_offset >= 0) ? P.nodecache + s.nc_offset : nullptr;
     const int np = s.npart, nsec = s.nsec, M = s.nslice, L = s.nlevel;
     for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
-    for (int a = 0; a < P.nattempt; ++a) {
+    const int nat = P.nattempt_r ? P.nattempt_r[r] : P.nattempt;
+    for (int a = 0; a < nat; ++a) {
       const uint32_t att = att0 + (uint32_t)a;
       // ---- section choice and moving particle
       if (threadIdx.x == 0) {
         int i1, i2 = -2;
         uint32_t ui = 0;
-        const double x = stream_uniform(P.seed, r, att, ui++) * (1 - 1e-8);
+        const double x = stream_uniform(P.seed, s.stream_id, att, ui++) * (1 - 1e-8);
         if (!s.fixed_node) {
           const int ilo = -1, ihi = M - 1;
           i1 = ilo + (int)((ihi + 1 - ilo) * x);
@@ -492,10 +504,10 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
           const int ilo = -1, ihi = M / 2 - 1;
           i1 = ilo + (int)((ihi + 1 - ilo) * x);
           if (i1 > ihi) i1 = ihi;
-          if (stream_uniform(P.seed, r, att, ui++) >= 0.5) i1 = (i1 + M / 2 + 1) % M - 1;
+          if (stream_uniform(P.seed, s.stream_id, att, ui++) >= 0.5) i1 = (i1 + M / 2 + 1) % M - 1;
           i2 = (i1 + M / 2 + 1) % M - 1;
         }
-        int ip = (int)(np * stream_uniform(P.seed, r, att, ui++));
+        int ip = (int)(np * stream_uniform(P.seed, s.stream_id, att, ui++));
         if (ip >= np) ip = np - 1;
         m.ictl[C_IFIRST1] = i1;
         m.ictl[C_IFIRST2] = i2;
@@ -523,7 +535,7 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
       int reject = -1;
       for (int level = L; level >= 0; --level) {
         const uint32_t ubase = level_uniform_base(s, level);
-        const double lnT = mover_level(s, m, ipart, level, P.seed, r, att, ubase);
+        const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
         double ds = block_sum(action_partial(s, m, ipart, level), m.red);
         if (s.ewald && s.coulomb && level == 0) {
           for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
@@ -536,7 +548,7 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
           const uint32_t uacc =
               ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
           const double p = exp(lnT + (-total + oldDS));
-          const double u = stream_uniform(P.seed, r, att, uacc);
+          const double u = stream_uniform(P.seed, s.stream_id, att, uacc);
           if (rec) {
             rec->ds[level] = ds;
             rec->ds_node[level] = dsn;
@@ -571,7 +583,10 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
             double* e = cache_entry(s, cache, msp, t1);
             e[2 + j] = m.ndist[(k * 2) * nsm + j];
             e[2 + n + j] = m.ndist[(k * 2 + 1) * nsm + j];
-            if (sho) e[2 + 2 * n + jcol * n + j] = m.ncol[k * nsm + j];
+            const double* nc = m.ncol + k * m.ncol_stride;
+            e[2 + 2 * n + jcol * n + j] = nc[j];
+            if (!sho)
+              for (int c = 1; c < 4; ++c) e[2 + 2 * n + c * n * n + jcol * n + j] = nc[c * n + j];
           }
           __syncthreads();
           for (int k = 1 + threadIdx.x; k < nsec - 1; k += blockDim.x) {
@@ -605,10 +620,10 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
       __syncthreads();
     }
     if (threadIdx.x == 0) {
-      P.state[r].attempt = att0 + (uint32_t)P.nattempt;
+      P.state[r].attempt = att0 + (uint32_t)nat;
       P.state[r].status = status;
       P.state[r].accepted += nacc;
-      P.state[r].attempted += P.nattempt;
+      P.state[r].attempted += nat;
       for (int k = 0; k < kMaxSpecies; ++k) {
         P.state[r].node_scale[k] = scale[k];
         P.state[r].epoch[k] = epoch[k];
@@ -624,7 +639,8 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
 // SpringAction (src/action/SpringAction.cc:112-123), SHOAction
 // (src/action/SHOAction.cc:71-105), PrimSHOAction (src/action/PrimSHOAction.cc:66-81),
 // PairAction (src/action/PairAction.cc:509-599).  The Ewald term is added per slice.
-__device__ double link_utau(const DevSys& s, const double* path, int ip, int t) {
+__device__ double link_utau(const DevSys& s, const double* path, int ip, int t,
+                            bool with_pairs = true) {
   const int np = s.npart, M = s.nslice;
   const int tm = t == 0 ? M - 1 : t - 1;
   const double* b1 = path + ((size_t)t * np + ip) * 3;
@@ -653,7 +669,7 @@ __device__ double link_utau(const DevSys& s, const double* path, int ip, int t) 
     const double x2 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
     utau += s.prim_a[sp] * x2 + s.prim_b[sp] * x2 * x2;
   }
-  if (s.coulomb) {
+  if (s.coulomb && with_pairs) {
     double uc = 0.0;
     for (int ti = 0; ti < s.ntab; ++ti) {
       const DevTable& tb = s.tab[ti];
@@ -705,6 +721,7 @@ __device__ double link_utau(const DevSys& s, const double* path, int ip, int t) 
 
 struct ThermoParams {
   const DevSys* sys;
+  const int* index;  // replicas to measure (null: all, blockIdx.y)
   const double* paths;
   double* partial;  // [nrep][nchunk]
   int nchunk;
@@ -712,13 +729,106 @@ struct ThermoParams {
   Layout lay;
 };
 
+// True when the minimum image of -v is not the negative of v's (a component
+// exactly at half a box length, where the image rounding breaks the tie
+// one way): the pair term then differs between the two orderings.
+__device__ __forceinline__ bool pbc_tie(const DevSys& s, double x, double y, double z) {
+  if (!(dot3(x, y, z, x, y, z) > s.rcut2)) return false;
+  const double v[3] = {x, y, z};
+  for (int d = 0; d < 3; ++d) {
+    const double ip = floor(__dadd_rn(__dmul_rn(s.cellb[d], v[d]), 1000.5)) - 1000;
+    const double im = floor(__dadd_rn(__dmul_rn(s.cellb[d], -v[d]), 1000.5)) - 1000;
+    if (im != -ip) return true;
+  }
+  return false;
+}
+
+// utau of the ordered pair (i, j) on the link ending at slice t (PairAction's
+// derivative term of the Coulomb pair action, src/action/PairAction.cc:509-599).
+__device__ double pair_utau_ordered(const DevSys& s, const DevTable& tb, const double* path, int i,
+                                    int j, int t) {
+  const int np = s.npart, M = s.nslice;
+  const int tm = t == 0 ? M - 1 : t - 1;
+  const double* b1 = path + ((size_t)t * np + i) * 3;
+  const double* b0 = path + ((size_t)tm * np + i) * 3;
+  const double* c1 = path + ((size_t)t * np + j) * 3;
+  const double* c0 = path + ((size_t)tm * np + j) * 3;
+  double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
+  pbc(s, ex, ey, ez);
+  double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
+  pbc(s, px, py, pz);
+  if (s.mixed) {
+    const float fx = (float)ex, fy = (float)ey, fz = (float)ez;
+    const float gx = (float)px, gy = (float)py, gz = (float)pz;
+    const float r = sqrtf(fx * fx + fy * fy + fz * fz);
+    const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
+    const float q = 0.5f * (r + rp);
+    const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
+    const float s2 = __fdividef(sx * sx + sy * sy + sz * sz, q * q);
+    return (double)tab_uk0d_tau_f(tb, q, s2);
+  }
+  const double r = sqrt(dot3(ex, ey, ez, ex, ey, ez));
+  const double rp = sqrt(dot3(px, py, pz, px, py, pz));
+  const double q = 0.5 * (r + rp);
+  const double sx = ex - px, sy = ey - py, sz = ez - pz;
+  const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (q * q);
+  double v, vt;
+  tab_uk0d(tb, q, s2, v, vt);
+  return vt;
+}
+
+// The pair's share of Σ_links utau: pi-qmc adds 0.5 utau for each ordering
+// (PairAction::getBeadAction runs over every partner of every particle); the two
+// orderings agree unless an image tie makes them differ, so one evaluation
+// usually stands for both.
+__device__ double pair_utau(const DevSys& s, const DevTable& tb, const double* path, int i, int j,
+                            int t) {
+  const int np = s.npart, M = s.nslice;
+  const int tm = t == 0 ? M - 1 : t - 1;
+  const double* b1 = path + ((size_t)t * np + i) * 3;
+  const double* b0 = path + ((size_t)tm * np + i) * 3;
+  const double* c1 = path + ((size_t)t * np + j) * 3;
+  const double* c0 = path + ((size_t)tm * np + j) * 3;
+  const bool tie = pbc_tie(s, b1[0] - c1[0], b1[1] - c1[1], b1[2] - c1[2]) ||
+                   pbc_tie(s, b0[0] - c0[0], b0[1] - c0[1], b0[2] - c0[2]);
+  const double a = pair_utau_ordered(s, tb, path, i, j, t);
+  if (!tie) return a;
+  return 0.5 * a + 0.5 * pair_utau_ordered(s, tb, path, j, i, t);
+}
+
+// Pair k of round rd of the round-robin schedule over n (even) players: every
+// round pairs all players once, so a flat (round, k) index covers each
+// unordered pair exactly once without a triangular index.
+__device__ __forceinline__ void round_robin_pair(int n, int rd, int k, int& a, int& b) {
+  const int m = n - 1;
+  if (k == 0) {
+    a = m;
+    b = rd;
+  } else {
+    a = (rd + k) % m;
+    b = (rd - k + m) % m;
+  }
+}
+
+// Per-replica energy from the chunk partials: chunks summed in order, then
+// divided by the slice count (ThermoEnergyEstimator's normalisation).
+__global__ void thermo_reduce_kernel(const DevSys* sys, const int* index, const double* partial,
+                                     int nchunk, int nrow, double* energy) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nrow) return;
+  const int r = index ? index[k] : k;
+  double s = 0.0;
+  for (int c = 0; c < nchunk; ++c) s = __dadd_rn(s, partial[(size_t)k * nchunk + c]);
+  energy[r] = __ddiv_rn(s, (double)sys[r].nslice);
+}
+
 // One CTA per (chunk of slices, replica): link utau sums plus, for Coulomb with
 // Ewald, the long-range energy of each slice (CoulombAction::getBeadAction adds
 // it at ipart == 0, src/action/CoulombAction.cc:165-171).
 __global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
   extern __shared__ double smem[];
   __shared__ DevSys S;
-  const int r = blockIdx.y;
+  const int r = P.index ? P.index[blockIdx.y] : blockIdx.y;
   {
     const int* src = (const int*)(P.sys + r);
     int* dst = (int*)&S;
@@ -732,10 +842,35 @@ __global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
   const int per = (M + P.nchunk - 1) / P.nchunk;
   const int t0 = blockIdx.x * per, t1 = min(M, t0 + per);
   Smem m = carve(smem, P.lay, s, nullptr);
+  // table of each species pair (pairs with no table contribute nothing)
+  __shared__ signed char tabof[kMaxSpecies][kMaxSpecies];
+  if (threadIdx.x < kMaxSpecies * kMaxSpecies) {
+    const int a = threadIdx.x / kMaxSpecies, b = threadIdx.x % kMaxSpecies;
+    int ti = -1;
+    for (int k = 0; k < s.ntab; ++k)
+      if ((s.tab[k].s1 == a && s.tab[k].s2 == b) || (s.tab[k].s1 == b && s.tab[k].s2 == a)) ti = k;
+    tabof[a][b] = (signed char)ti;
+  }
+  __syncthreads();
   double part = 0.0;
   for (int it = threadIdx.x; it < (t1 - t0) * np; it += blockDim.x) {
     const int t = t0 + it / np, ip = it % np;
-    part += link_utau(s, path, ip, t);
+    part += link_utau(s, path, ip, t, false);
+  }
+  if (s.coulomb && np > 1) {
+    // every pair once per slice: rounds of the round-robin schedule (np rounded up to even)
+    const int ne = np + (np & 1), per_round = ne / 2, nrd = ne - 1;
+    const int items = (t1 - t0) * nrd * per_round;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int t = t0 + it / (nrd * per_round);
+      const int rest = it % (nrd * per_round);
+      int a, b;
+      round_robin_pair(ne, rest / per_round, rest % per_round, a, b);
+      if (a >= np || b >= np) continue;  // the bye of an odd count
+      const int ti = tabof[species_of(s, a)][species_of(s, b)];
+      if (ti < 0) continue;
+      part += pair_utau(s, s.tab[ti], path, a, b, t);
+    }
   }
   double tot = block_sum(part, m.red);
   if (s.coulomb && s.ewald) {
@@ -759,7 +894,7 @@ __global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
       tot += d / s.epsilon;
     }
   }
-  if (threadIdx.x == 0) P.partial[(size_t)r * P.nchunk + blockIdx.x] = tot;
+  if (threadIdx.x == 0) P.partial[(size_t)blockIdx.y * P.nchunk + blockIdx.x] = tot;
 }
 
 // ------------------------------------------------------- Action-level entry
@@ -893,10 +1028,11 @@ __global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, 
 namespace pimc {
 
 // ------------------------------------------- allocation-free node evaluation
-// Scratch for node_eval_noalloc_kernel: one slot of 3 * 32 * 32 + 33 doubles
-// (rounded up to 3136: the LU, inverse and exp matrices and pivot reciprocals
-// of one Slater matrix of up to 32 particles) per resident warp, kNoAllocSlots
-// slots: 3.1 MiB, held by every GPU that loads the library until exit.
+// Scratch for node_eval_noalloc_kernel: one slot of 6 * 32 * 32 + 33 doubles
+// (rounded up to 6208: the LU, inverse and exp matrices, pivot reciprocals and
+// the three gradient matrices of free-particle nodes, for one Slater matrix of
+// up to 32 particles) per resident warp, kNoAllocSlots slots: 6.1 MiB, held by
+// every GPU that loads the library until exit.
 constexpr int kNoAllocSlots = 128;
 constexpr int kNoAllocSlot = (node_group_scratch(kMaxNs) + 31) / 32 * 32;
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocSlots * kNoAllocSlot];

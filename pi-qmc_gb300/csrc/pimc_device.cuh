@@ -30,6 +30,7 @@ struct DevSys {
   double sho_omega[kMaxSpecies], prim_a[kMaxSpecies], prim_b[kMaxSpecies];
   int node_kind[kMaxSpecies];
   double node_c[kMaxSpecies], node_cosh[kMaxSpecies];  // SHONodes constants
+  double node_dk[kMaxSpecies];  // sqrt(2 m / tau): nodal distance = node_dk / |grad ln det|
   // FreeParticleNodes: PeriodicGaussian(alpha = m T, L) per species and axis.
   double pg_nome[kMaxSpecies][3], pg_pref[kMaxSpecies][3], pg_k[kMaxSpecies][3];
   int pg_nmax[kMaxSpecies][3];
@@ -54,6 +55,7 @@ struct DevSys {
   double one_over_2v, self_energy, deltak[3];
   int ikmax[3];
   int ns_max;           // largest node-species count
+  uint32_t stream_id;     // random stream of this replica (its replica or request id)
   long long nc_offset;    // doubles into the Slater-result cache pool (-1: no cache)
   int nc_stride;          // doubles per cache entry
   long long path_offset;  // doubles into the path pool

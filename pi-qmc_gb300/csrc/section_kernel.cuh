@@ -33,7 +33,8 @@ struct Smem {
   int* ictl;                // control words
   double* nodescr;          // per-warp node scratch (smem or global)
   double* ecache;           // [nsec][n*n] exp matrices of the moving species (SHONodes)
-  double* ncol;             // [nsec][ns_max] recomputed exp column of each changed slice
+  double* ncol;             // [nsec][ncol_stride] recomputed column of each changed slice
+  int ncol_stride;          // ns_max (SHO exp column) or 4 ns_max (free-particle values + gradients)
   int nodescr_stride;       // doubles per warp
 };
 
@@ -90,10 +91,11 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
   const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
   const int f = s.spec_first[sp];
-  double* A = scr;          // n*n column-major, LU
+  double* A = scr;          // n*n column-major, LU; after the inverse: the distance weights
   double* X = A + n * n;    // n*n inverse, column-major
   double* E = X + n * n;    // n*n exp values (SHO nodes)
   double* R = E + n * n;    // n reciprocals of the U diagonal
+  double* G = R + n + 1;    // 3 n*n gradient factors (free-particle nodes)
   const bool sho = s.node_kind[sp] == 1;
   // --- build the Slater matrix: A(i,j) = scale * rho(r1_j, r2_i)
   if (gl < n) {
@@ -119,30 +121,69 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
         A[j * n + gl] = scale * e;
       }
     } else {
+      // values rho = v0 v1 v2 and, for the distances, the gradient of each
+      // element with respect to r1_j (the r2_i gradient is its negative); a
+      // column update reads the unchanged columns from ecache ([4][n][n]:
+      // values, then the three gradient components)
+      const int nn = n * n;
       for (int j = 0; j < n; ++j) {
-        double rjx, rjy, rjz;
-        v1.get(f + j, rjx, rjy, rjz);
-        double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
-        pbc(s, dx, dy, dz);
-        double g, ear2 = scale;
-        ear2 *= pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g);
-        ear2 *= pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g);
-        ear2 *= pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g);
-        A[j * n + gl] = ear2;
+        double val, gx, gy, gz;
+        if (ecache && jcol >= 0 && j != jcol) {
+          val = ecache[j * n + gl];
+          gx = ecache[nn + j * n + gl];
+          gy = ecache[2 * nn + j * n + gl];
+          gz = ecache[3 * nn + j * n + gl];
+        } else {
+          double rjx, rjy, rjz;
+          v1.get(f + j, rjx, rjy, rjz);
+          double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
+          pbc(s, dx, dy, dz);
+          double g0, g1, g2;
+          const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
+          const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
+          const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
+          val = v0 * v1v * v2v;
+          gx = g0 / (v0 + 1e-300);
+          gy = g1 / (v1v + 1e-300);
+          gz = g2 / (v2v + 1e-300);
+          gx *= v0; gy *= v0; gz *= v0;
+          gx *= v1v; gy *= v1v; gz *= v1v;
+          gx *= v2v; gy *= v2v; gz *= v2v;
+          if (ecache && jcol < 0 && write) {
+            ecache[j * n + gl] = val;
+            ecache[nn + j * n + gl] = gx;
+            ecache[2 * nn + j * n + gl] = gy;
+            ecache[3 * nn + j * n + gl] = gz;
+          }
+          if (newcol && j == jcol && write) {
+            newcol[gl] = val;
+            newcol[n + gl] = gx;
+            newcol[2 * n + gl] = gy;
+            newcol[3 * n + gl] = gz;
+          }
+        }
+        A[j * n + gl] = scale * val;
+        G[j * n + gl] = gx;
+        G[nn + j * n + gl] = gy;
+        G[2 * nn + j * n + gl] = gz;
       }
     }
   }
   __syncwarp();
-  // --- LU with partial pivoting
+  // --- LU with partial pivoting (the pivot is the first largest |a|)
   int info = 0;
   unsigned pivbits = 0;  // bit j set: row j was interchanged
   int piv_lane = gl;     // piv[gl] for gl < n
   for (int j = 0; j < n; ++j) {
-    double av = (gl >= j && gl < n) ? fabs(A[j * n + gl]) : -1.0;
+    // |a| compared through its bit pattern (monotonic for non-negative
+    // doubles), so the search runs on the integer pipe; -1 marks idle lanes
+    long long av = (gl >= j && gl < n)
+                       ? (__double_as_longlong(A[j * n + gl]) & 0x7fffffffffffffffLL)
+                       : -1LL;
     int ai = gl;
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) {
-      const double ov = __shfl_down_sync(FULL, av, o, W);
+      const long long ov = __shfl_down_sync(FULL, av, o, W);
       const int oi = __shfl_down_sync(FULL, ai, o, W);
       if (ov > av || (ov == av && oi < ai)) {
         av = ov;
@@ -169,9 +210,21 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
       info = j + 1;
     }
     __syncwarp();
-    if (gl > j && gl < n) {
-      const double lij = A[j * n + gl];
-      for (int k = j + 1; k < n; ++k) A[k * n + gl] -= lij * A[k * n + j];
+    // trailing update, one element per lane and step: a(i,k) -= l(i,j) u(j,k)
+    const int m = n - j - 1;
+    if (m > 0) {
+      int kk = gl / m, ii = gl - kk * m;
+      const int dk = W / m, di = W - dk * m;
+      for (int e = gl; e < m * m; e += W) {
+        const int row = j + 1 + ii, col = j + 1 + kk;
+        A[col * n + row] -= A[j * n + row] * A[col * n + j];
+        ii += di;
+        kk += dk;
+        if (ii >= m) {
+          ii -= m;
+          ++kk;
+        }
+      }
     }
     __syncwarp();
   }
@@ -209,95 +262,108 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
     }
   }
   __syncwarp();
-  // --- nodal distances.  inv(j,i) = X[i*n + j].  (No early exit: a singular
-  // group simply skips them, so the warp stays converged.)
-  const double twom_tau = 2 * s.mass[sp];
+  // --- nodal distances: d = sqrt(2m / (tau |grad ln det|^2)), the gradient
+  // with respect to r1_j (d1) and r2_i (d2); inv(j,i) = X[i*n + j].  (No early
+  // exit: a singular group simply skips them, so the warp stays converged.)
+  const double dk = s.node_dk[sp];
   const bool ok = info == 0;
-  if (ok && gl < n) {
-    const int j = gl;  // d1: gradient with respect to r1_j
-    double rjx, rjy, rjz;
-    v1.get(f + j, rjx, rjy, rjz);
-    double lx = 0, ly = 0, lz = 0;
-    for (int i = 0; i < n; ++i) {
-      double rix, riy, riz;
-      v2.get(f + i, rix, riy, riz);
-      double gx, gy, gz;
-      if (sho) {
-        const double c = s.node_c[sp], ch = s.node_cosh[sp];
-        const double e = E[j * n + i];
-        gx = 2 * c * (rix - ch * rjx) * e;
-        gy = 2 * c * (riy - ch * rjy) * e;
-        gz = 2 * c * (riz - ch * rjz) * e;
-        const double w = X[i * n + j] * scale;
-        lx += w * gx;
-        ly += w * gy;
-        lz += w * gz;
-      } else {
-        double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
-        pbc(s, dx, dy, dz);
-        double g0, g1, g2;
-        const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
-        const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
-        const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
-        gx = g0 / (v0 + 1e-300);
-        gy = g1 / (v1v + 1e-300);
-        gz = g2 / (v2v + 1e-300);
-        gx *= v0; gy *= v0; gz *= v0;
-        gx *= v1v; gy *= v1v; gz *= v1v;
-        gx *= v2v; gy *= v2v; gz *= v2v;
-        const double w = X[i * n + j];
-        lx += w * gx * scale;
-        ly += w * gy * scale;
-        lz += w * gz * scale;
+  if (sho) {
+    // weights w(i,j) = inv(j,i) rho(i,j), shared by both gradients
+    if (ok) {
+      int j = gl / n, i = gl - j * n;
+      const int dj = W / n, di = W - dj * n;
+      for (int e = gl; e < n * n; e += W) {
+        A[j * n + i] = X[i * n + j] * E[j * n + i];
+        i += di;
+        j += dj;
+        if (i >= n) {
+          i -= n;
+          ++j;
+        }
       }
     }
-    if (write) d1[j] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
-  }
-  if (ok && gl < n) {
-    const int i = gl;  // d2: gradient with respect to r2_i
-    double rix, riy, riz;
-    v2.get(f + i, rix, riy, riz);
-    double lx = 0, ly = 0, lz = 0;
-    for (int j = 0; j < n; ++j) {
+    __syncwarp();
+    const double c = s.node_c[sp], ch = s.node_cosh[sp];
+    const double fac = 2 * c * scale;
+    if (ok && gl < n) {
+      const int j = gl;  // d1: sum_i w(i,j) 2c (r2_i - ch r1_j)
       double rjx, rjy, rjz;
       v1.get(f + j, rjx, rjy, rjz);
-      double gx, gy, gz;
-      if (sho) {
-        const double c = s.node_c[sp], ch = s.node_cosh[sp];
-        const double e = E[j * n + i];
-        gx = 2 * c * (rjx - ch * rix) * e;
-        gy = 2 * c * (rjy - ch * riy) * e;
-        gz = 2 * c * (rjz - ch * riz) * e;
-        const double w = X[i * n + j] * scale;
-        lx += w * gx;
-        ly += w * gy;
-        lz += w * gz;
-      } else {
-        double dx = rix - rjx, dy = riy - rjy, dz = riz - rjz;
-        pbc(s, dx, dy, dz);
-        double g0, g1, g2;
-        const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
-        const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
-        const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
-        gx = g0 / (v0 + 1e-300);
-        gy = g1 / (v1v + 1e-300);
-        gz = g2 / (v2v + 1e-300);
-        gx *= v0; gy *= v0; gz *= v0;
-        gx *= v1v; gy *= v1v; gz *= v1v;
-        gx *= v2v; gy *= v2v; gz *= v2v;
-        const double w = X[i * n + j];
-        lx += w * gx * scale;
-        ly += w * gy * scale;
-        lz += w * gz * scale;
+      const double cx = ch * rjx, cy = ch * rjy, cz = ch * rjz;
+      double lx = 0, ly = 0, lz = 0;
+      for (int i = 0; i < n; ++i) {
+        double rix, riy, riz;
+        v2.get(f + i, rix, riy, riz);
+        const double w = A[j * n + i];
+        lx += w * (rix - cx);
+        ly += w * (riy - cy);
+        lz += w * (riz - cz);
       }
+      lx *= fac;
+      ly *= fac;
+      lz *= fac;
+      if (write) d1[j] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
     }
-    if (write) d2[i] = sqrt(twom_tau / ((dot3(lx, ly, lz, lx, ly, lz) + 1e-15) * s.tau));
+    if (ok && gl < n) {
+      const int i = gl;  // d2: sum_j w(i,j) 2c (r1_j - ch r2_i)
+      double rix, riy, riz;
+      v2.get(f + i, rix, riy, riz);
+      const double cx = ch * rix, cy = ch * riy, cz = ch * riz;
+      double lx = 0, ly = 0, lz = 0;
+      for (int j = 0; j < n; ++j) {
+        double rjx, rjy, rjz;
+        v1.get(f + j, rjx, rjy, rjz);
+        const double w = A[j * n + i];
+        lx += w * (rjx - cx);
+        ly += w * (rjy - cy);
+        lz += w * (rjz - cz);
+      }
+      lx *= fac;
+      ly *= fac;
+      lz *= fac;
+      if (write) d2[i] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
+    }
+  } else {
+    const double* Gx = G;
+    const double* Gy = G + n * n;
+    const double* Gz = G + 2 * n * n;
+    if (ok && gl < n) {
+      const int j = gl;  // d1: sum_i inv(j,i) dA(i,j)/dr1_j
+      double lx = 0, ly = 0, lz = 0;
+      for (int i = 0; i < n; ++i) {
+        const double w = X[i * n + j];
+        lx += w * Gx[j * n + i];
+        ly += w * Gy[j * n + i];
+        lz += w * Gz[j * n + i];
+      }
+      lx *= scale;
+      ly *= scale;
+      lz *= scale;
+      if (write) d1[j] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
+    }
+    if (ok && gl < n) {
+      const int i = gl;  // d2: sum_j inv(j,i) dA(i,j)/dr2_i, dA/dr2_i = -dA/dr1_j
+      double lx = 0, ly = 0, lz = 0;
+      for (int j = 0; j < n; ++j) {
+        const double w = X[i * n + j];
+        lx += w * Gx[j * n + i];
+        ly += w * Gy[j * n + i];
+        lz += w * Gz[j * n + i];
+      }
+      lx *= scale;
+      ly *= scale;
+      lz *= scale;
+      if (write) d2[i] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
+    }
   }
   __syncwarp();
 }
 
-// Scratch doubles one lane group needs for an n-particle species.
-__host__ __device__ constexpr int node_group_scratch(int n) { return 3 * n * n + n + 1; }
+// Scratch doubles one lane group needs for an n-particle species (free-particle
+// nodes keep three gradient matrices besides the LU, inverse and exp matrices).
+__host__ __device__ constexpr int node_group_scratch(int n, bool free_nodes = true) {
+  return 3 * n * n + n + 1 + (free_nodes ? 3 * n * n : 0);
+}
 
 // Group width for an n-particle species.
 __host__ __device__ __forceinline__ int node_group_width(int n) {

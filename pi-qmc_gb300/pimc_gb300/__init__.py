@@ -19,6 +19,7 @@ MAXL = 6
 PIMC_NODES_NONE, PIMC_NODES_SHO, PIMC_NODES_FREE = 0, 1, 2
 PIMC_MOVER_FREE, PIMC_MOVER_FREE_PBC = 0, 1
 PIMC_PREC_FP64, PIMC_PREC_MIXED = 0, 1
+PIMC_ERR_CAPACITY = -4
 STATUS_BITS = {1: "init_crossing", 2: "singular", 4: "rescale_limit", 8: "nonfinite"}
 
 
@@ -49,6 +50,20 @@ class PairTable(C.Structure):
 class EwaldTable(C.Structure):
     _fields_ = [("totk", C.c_int), ("kvec", C.POINTER(C.c_int)), ("vk", C.POINTER(C.c_double)),
                 ("one_over_2v", C.c_double), ("self_energy", C.c_double), ("ikmax", C.c_int * 3)]
+
+
+class LaunchConfig(C.Structure):
+    _fields_ = [("block", C.c_int), ("scratch_global", C.c_int), ("ctas_per_sm", C.c_int),
+                ("ms", C.c_float)]
+
+    def as_dict(self):
+        return {"block": self.block, "scratch_global": self.scratch_global,
+                "ctas_per_sm": self.ctas_per_sm, "ms": round(float(self.ms), 4)}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("hbm_bytes", C.c_size_t), ("max_npart", C.c_int),
+                ("max_nslice", C.c_int), ("max_level", C.c_int), ("max_node_count", C.c_int)]
 
 
 class MoveRecord(C.Structure):
@@ -115,6 +130,7 @@ def lib():
         L.pimc_replica_status.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                           C.POINTER(C.c_uint32)]
         L.pimc_thermo_energy.argtypes = [P, D]
+        L.pimc_run_steps.argtypes = [P, I, I, D]
         L.pimc_action_difference.argtypes = [P, I, I, D, D, C.POINTER(C.c_int), D]
         L.pimc_node_evaluate.argtypes = [P, I, I, D, D, D, D, D, C.POINTER(C.c_int)]
         L.pimc_node_scale.argtypes = [P, I, I, D]
@@ -122,6 +138,18 @@ def lib():
         L.pimc_fp64_peak.argtypes = [D]
         L.pimc_node_evaluate_noalloc.argtypes = [C.POINTER(System), I, C.c_double, I, P, P, P,
                                                  P, P, P, P]
+        L.pimc_engine_configure.argtypes = [P, C.POINTER(LaunchConfig)]
+        L.pimc_engine_get_config.argtypes = [P, C.POINTER(LaunchConfig)]
+        L.pimc_engine_autotune.argtypes = [P, I, C.POINTER(LaunchConfig),
+                                           C.POINTER(LaunchConfig), I, C.POINTER(C.c_int)]
+        L.pimc_server_create.argtypes = [C.POINTER(ServerConfig), C.c_uint64, I, C.POINTER(P)]
+        L.pimc_server_admit.argtypes = [P, C.POINTER(System), C.POINTER(PairTable), I, D,
+                                        C.c_uint32, I, C.POINTER(C.c_int)]
+        L.pimc_server_release.argtypes = [P, I]
+        L.pimc_server_run.argtypes = [P]
+        L.pimc_server_energy.argtypes = [P, D]
+        L.pimc_server_download_path.argtypes = [P, I, D]
+        L.pimc_server_pool.argtypes = [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.pimc_kernel_launches.argtypes = [P]
         L.pimc_kernel_launches.restype = C.c_int64
         _lib = L
@@ -294,6 +322,37 @@ class Engine:
         _check(lib().pimc_run_sections(self.h, nattempt, None))
         return None
 
+    def run_steps(self, nattempt, nsteps=1, energies=True):
+        """nsteps x (nattempt attempts + one energy measurement) as one CUDA
+        graph; returns energies [nsteps][nreplica] (or None, asynchronous)."""
+        if energies:
+            out = np.empty((nsteps, self.nreplica))
+            _check(lib().pimc_run_steps(self.h, nattempt, nsteps, _dp(out)))
+            return out
+        _check(lib().pimc_run_steps(self.h, nattempt, nsteps, None))
+        return None
+
+    # launch configuration --------------------------------------------------
+    def autotune(self, nattempt=16):
+        """Times the candidate launch configurations on nattempt attempts per
+        replica (the chains are restored), applies the fastest; returns it and
+        every candidate with its time (ms < 0: does not fit)."""
+        best = LaunchConfig()
+        tried = (LaunchConfig * 16)()
+        nt = C.c_int(0)
+        _check(lib().pimc_engine_autotune(self.h, nattempt, C.byref(best), tried, 16,
+                                          C.byref(nt)))
+        return best.as_dict(), [tried[i].as_dict() for i in range(min(nt.value, 16))]
+
+    def configure(self, block, scratch_global=0, ctas_per_sm=0):
+        cfg = LaunchConfig(block, scratch_global, ctas_per_sm, 0.0)
+        _check(lib().pimc_engine_configure(self.h, C.byref(cfg)))
+
+    def launch_config(self):
+        cfg = LaunchConfig()
+        _check(lib().pimc_engine_get_config(self.h, C.byref(cfg)))
+        return cfg.as_dict()
+
     def replica_status(self):
         n = self.nreplica
         acc = np.zeros(n, np.int64)
@@ -339,6 +398,94 @@ class Engine:
         return err, det, d1, d2
 
     @property
+    def kernel_launches(self):
+        return lib().pimc_kernel_launches(self.h)
+
+
+class Server:
+    """Slots of independent simulations over one device pool (pimc_server_*).
+
+    ``admit`` places a simulation in a free slot when its path and Slater-result
+    cache fit the pool (returns None when they do not), ``run`` advances every
+    admitted slot in one persistent launch, ``release`` frees the slot and its
+    memory.  Each simulation draws the random stream of its own ``stream_id``.
+    """
+
+    def __init__(self, slots, hbm_bytes, max_npart, max_nslice, max_level, max_node_count,
+                 seed=20261203, precision=PIMC_PREC_FP64):
+        L = lib()
+        cfg = ServerConfig(slots, hbm_bytes, max_npart, max_nslice, max_level, max_node_count)
+        h = C.c_void_p()
+        _check(L.pimc_server_create(C.byref(cfg), C.c_uint64(seed), precision, C.byref(h)))
+        self.h = h
+        self.slots = slots
+        self.systems = [None] * slots
+        self._keep = [None] * slots
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pimc_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib().pimc_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def admit(self, system_kw, tables, path, stream_id, round_attempts):
+        sysc = system_from_kw(system_kw)
+        tabs, keep = pair_tables_struct(tables)
+        flat = np.ascontiguousarray(path, np.float64).ravel()
+        assert flat.size == 3 * sysc.nslice * sysc.npart
+        slot = C.c_int(-1)
+        rc = lib().pimc_server_admit(self.h, C.byref(sysc), tabs, len(tables), _dp(flat),
+                                     C.c_uint32(stream_id), int(round_attempts), C.byref(slot))
+        if rc == PIMC_ERR_CAPACITY:
+            return None
+        _check(rc)
+        self.systems[slot.value] = sysc
+        self._keep[slot.value] = (keep, tables)
+        return slot.value
+
+    def release(self, slot):
+        _check(lib().pimc_server_release(self.h, slot))
+        self.systems[slot] = None
+        self._keep[slot] = None
+
+    def run(self):
+        """One round: every slot advances its own round_attempts."""
+        _check(lib().pimc_server_run(self.h))
+
+    def energies(self):
+        out = np.empty(self.slots)
+        _check(lib().pimc_server_energy(self.h, _dp(out)))
+        return out
+
+    def download_path(self, slot):
+        s = self.systems[slot]
+        out = np.empty((s.nslice, s.npart, 3))
+        _check(lib().pimc_server_download_path(self.h, slot, _dp(out)))
+        return out
+
+    def pool(self):
+        used, big = C.c_size_t(), C.c_size_t()
+        _check(lib().pimc_server_pool(self.h, C.byref(used), C.byref(big)))
+        return used.value, big.value
+
+    def replica_status(self):
+        n = self.slots
+        acc = np.zeros(n, np.int64)
+        att = np.zeros(n, np.int64)
+        st = np.zeros(n, np.uint32)
+        _check(lib().pimc_replica_status(self.h, acc.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         att.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         st.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return acc, att, st
+
     def kernel_launches(self):
         return lib().pimc_kernel_launches(self.h)
 

@@ -113,3 +113,39 @@ def tables_for(kw, base_tables):
             if i != j or counts[i] > 1:
                 out.append(by[(i, j)])
     return out
+
+
+def serve_stream(nreq, rate=200.0, seed=DEFAULT_SEED, sweep_scale=1e-4, nmin=2, nmax=64,
+                 slices=(64, 128, 256, 512, 1024, 2048), sweeps=(1e3, 1e5), omega=(0.5, 2.0),
+                 tau=1.0 / 25.6):
+    """A stream of dot simulations arriving as a Poisson process of `rate`
+    requests/s: N uniform in {nmin..nmax} (ceil(N/2) up, floor(N/2) down,
+    SHONodes per spin, node temperature omega/4), omega uniform in [0.5, 2],
+    M uniform over `slices`, beta = M tau, level 4 for M <= 128 else 5, requested
+    sweeps log-uniform in `sweeps` and multiplied by `sweep_scale`.
+
+    Returns [(arrival_seconds, system_kw, sweeps)], sweeps a float >= 0."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for _ in range(nreq):
+        t += float(rng.exponential(1.0 / rate))
+        n = int(rng.integers(nmin, nmax + 1))
+        w = float(rng.uniform(*omega))
+        m = int(rng.choice(slices))
+        lev = 4 if m <= 128 else 5
+        sw = math.exp(rng.uniform(math.log(sweeps[0]), math.log(sweeps[1]))) * sweep_scale
+        up, dn = (n + 1) // 2, n // 2
+        counts = [up, dn] if dn > 0 else [up]
+        ns = len(counts)
+        kw = dict(counts=counts, sho_omega=[w] * ns, nslice=m, beta=m * tau, nlevel=lev,
+                  coulomb=1, norder=3, node_kind=[1] * ns, node_omega=[w] * ns,
+                  node_temperature=w / 4.0, cell=DOT_CELL)
+        out.append((t, kw, sw))
+    return out
+
+
+def sweep_attempts(kw):
+    """Section attempts of one sweep: every particle's path covered once by
+    non-overlapping sections, N M / 2^L attempts."""
+    return max(1, sum(kw["counts"]) * kw["nslice"] // (1 << kw["nlevel"]))

@@ -208,3 +208,66 @@ def test_uneven_batch_matches_checker(pimc):
         assert rel_close(pr["ds_node"], rec["ds_node"][r][:, :9], 1e-9)
         assert np.abs(port.get_path() - out[r]).max() <= 1e-12
         assert E[r] == pytest.approx(port.thermo_energy(), rel=1e-12)
+
+
+def test_graph_steps_equal_direct_calls(pimc):
+    # The captured step graph (sweep + energy measurement, replayed) is the same
+    # work as the direct calls: energies and paths bit for bit, and a replay
+    # continues the chain.
+    g = golden_io.load("dot4_fn")
+    a = engine_for(pimc, g, nreplica=3)
+    b = engine_for(pimc, g, nreplica=3)
+    for e in (a, b):
+        e.upload_paths([g["path0"]] * 3)
+    ea = np.concatenate([a.run_steps(20, 3), a.run_steps(20, 3)])
+    eb = []
+    for _ in range(6):
+        b.run_sections(20)
+        eb.append(b.thermo_energy())
+    assert np.array_equal(ea, np.array(eb))
+    for pa, pb in zip(a.download_paths(), b.download_paths()):
+        assert np.array_equal(pa, pb)
+    n0 = a.kernel_launches
+    a.run_steps(20, 3, energies=False)
+    assert a.kernel_launches - n0 == 9
+
+
+@pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small"])
+@pytest.mark.parametrize("block,scratch_global", [(64, 0), (128, 1), (256, 1)])
+def test_launch_configs_match_golden(pimc, case, block, scratch_global):
+    # Every launch configuration the autotuner may pick reproduces pi-qmc's
+    # decisions and action differences.
+    g = golden_io.load(case)
+    e = engine_for(pimc, g)
+    fixed = any(g["kw"].get("node_kind", [0]))
+    e.configure(block, scratch_global if fixed else 0)
+    e.upload_paths([g["path0"]])
+    n = min(g["nattempt"], 200)
+    rec = e.run_sections(n, records=True)
+    ref = g["records"]
+    for k in ("ifirst1", "ipart", "reject_level"):
+        assert np.array_equal(rec[k][0], ref[k][:n]), k
+    nl = g["kw"]["nlevel"] + 1
+    assert rel_close(rec["ds"][0][:, :nl], ref["ds"][:n, :nl], 1e-12)
+    assert rel_close(rec["ds_node"][0][:, :nl], ref["ds_node"][:n, :nl], NODE_TOL.get(case, 1e-10))
+
+
+def test_autotune_does_not_advance_chains(pimc):
+    g = golden_io.load("dot4_fn")
+    a = engine_for(pimc, g, nreplica=8)
+    b = engine_for(pimc, g, nreplica=8)
+    for e in (a, b):
+        e.upload_paths([g["path0"]] * 8)
+    best, tried = a.autotune(8)
+    assert len(tried) >= 3 and all(t["ms"] != 0 for t in tried)
+    assert best["ms"] > 0 and best["ms"] == min(t["ms"] for t in tried if t["ms"] > 0)
+    acc, att, st = a.replica_status()
+    assert att.sum() == 0
+    assert a.launch_config()["block"] == best["block"]
+    b.configure(best["block"], best["scratch_global"], best["ctas_per_sm"])
+    ra = a.run_sections(40, records=True)
+    rb = b.run_sections(40, records=True)
+    assert np.array_equal(ra["reject_level"], rb["reject_level"])
+    assert np.array_equal(ra["ds"], rb["ds"])
+    for pa, pb in zip(a.download_paths(), b.download_paths()):
+        assert np.array_equal(pa, pb)
