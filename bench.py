@@ -82,7 +82,7 @@ def init_kind(name):
 
 def defaults(name):
     # replicas per GPU and attempts per replica per step (0: one sweep)
-    return {"dot20_fn": (608, 0), "dot2": (9728, 0), "heg54": (152, 1),
+    return {"dot20_fn": (608, 0), "dot2": (9728, 0), "heg54": (152, 64),
             "batch4096": (4096, 32), "serve": (64, 64)}[name]
 
 
@@ -421,7 +421,8 @@ def run_engine(args, rank, world):
         else:
             ref = pimc_gb300.Engine(kw, R, tabs, ew, seed=seed)
         ref.set_stream(stream.cuda_stream)
-        ref.configure(tuned["block"], tuned["scratch_global"], tuned["ctas_per_sm"])
+        ref.configure(tuned["block"], tuned["scratch_global"], tuned["ctas_per_sm"],
+                      tuned["regs_variant"])
         ref.upload_paths(paths)          # the same history as the measured engine:
         ref.run_sections(4)              # depth-statistics attempts, re-upload,
         ref.upload_paths(paths)          # warm-up and timed steps
@@ -432,8 +433,10 @@ def run_engine(args, rank, world):
         energy_block["fp64"] = e64
         diff = energy_block["value"] - e64["value"]
         energy_block["diff_vs_fp64"] = diff
-        energy_block["diff_over_fp64_sigma"] = diff / e64["stat_err"] if e64["stat_err"] else None
-        energy_block["within_2sigma_of_fp64"] = bool(abs(diff) <= 2 * e64["stat_err"])
+        sig = math.hypot(e64["stat_err"] or 0.0, energy_block["stat_err"] or 0.0)
+        energy_block["diff_over_sigma"] = diff / sig if sig else None
+        energy_block["within_2sigma_of_fp64"] = bool(abs(diff) <= 2 * sig)
+        energy_block["sigma"] = "combined: sqrt(stat_err^2 + fp64 stat_err^2)"
     # ---- the plain form: one replica, FP64, same sweep (untimed by the step loop)
     plain = None if batch else pimc_gb300.Engine(kw, 1, tabs, ew, seed=seed)
     plain_value = None

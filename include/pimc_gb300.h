@@ -183,7 +183,8 @@ int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy
 
 /* Launch configuration of an engine's section kernel: threads per replica
  * (64, 128 or 256), the per-warp Slater scratch in shared (0) or global (1)
- * memory, and the replicas resident per SM (0: as many as fit).  ms is the
+ * memory, the replicas resident per SM (0: as many as fit) and the section
+ * kernel's register-budget variant.  ms is the
  * time the autotuner measured for it (0 when not measured).  A configuration
  * changes how per-thread partial sums are grouped, so chains run under two
  * configurations agree to rounding, not bit for bit. */
@@ -191,6 +192,7 @@ typedef struct {
   int block;
   int scratch_global;
   int ctas_per_sm;
+  int regs_variant;  /* register budget: 65536 / (256 * regs_variant) per thread (2, 3 or 4; 0 = 2) */
   float ms;
 } pimc_launch_config;
 

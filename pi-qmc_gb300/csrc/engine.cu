@@ -11,9 +11,39 @@
 #include <vector>
 
 #include "../../include/pimc_gb300.h"
+#include "entry_kernels.cuh"
 #include "kernels.cuh"
+#include "noalloc_kernel.cuh"
+
+namespace pimc {
+// register-budget variants of the section kernel (section_variants.cu)
+cudaError_t section_launch_v2(int, int, size_t, cudaStream_t, const RunParams&);
+cudaError_t section_launch_v3(int, int, size_t, cudaStream_t, const RunParams&);
+cudaError_t section_launch_v4(int, int, size_t, cudaStream_t, const RunParams&);
+int section_occupancy_v2(int, size_t);
+int section_occupancy_v3(int, size_t);
+int section_occupancy_v4(int, size_t);
+void section_smem_cap_v2(int);
+void section_smem_cap_v3(int);
+void section_smem_cap_v4(int);
+}  // namespace pimc
 
 using namespace pimc;
+
+namespace {
+// minb: 2, 3 or 4 resident 256-thread blocks per SM worth of registers
+cudaError_t section_launch(int minb, int grid, int block, size_t smem, cudaStream_t st,
+                           const RunParams& P) {
+  if (minb == 3) return section_launch_v3(grid, block, smem, st, P);
+  if (minb == 4) return section_launch_v4(grid, block, smem, st, P);
+  return section_launch_v2(grid, block, smem, st, P);
+}
+int section_occupancy(int minb, int block, size_t smem) {
+  if (minb == 3) return section_occupancy_v3(block, smem);
+  if (minb == 4) return section_occupancy_v4(block, smem);
+  return section_occupancy_v2(block, smem);
+}
+}  // namespace
 
 namespace {
 
@@ -101,6 +131,7 @@ struct pimc_engine {
   Layout lay{};
   LayoutOpts lay_opts{};
   int ctas_cap = 0;
+  int minb = 2;  // register-budget variant of the section kernel
   int block = kBlock;
   int grid = 0;
   int num_sms = 0;
@@ -310,12 +341,15 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.ncol = fixed ? take(nsec * L.ncol_stride) : -1;
   // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n) doubles
   int stride = 0;
-  bool anyfree = false;
+  // (the node species present decide it: a smaller species packs more lane
+  // groups per warp, so its per-warp scratch can be the larger one)
   for (const DevSys& d : sys)
-    for (int i = 0; i < d.nspecies; ++i) anyfree |= d.node_kind[i] == PIMC_NODES_FREE;
-  if (fixed)
-    for (int n = 1; n <= nsm; ++n)
-      stride = std::max(stride, (32 / node_group_width(n)) * node_group_scratch(n, anyfree));
+    for (int i = 0; i < d.nspecies; ++i)
+      if (d.node_kind[i]) {
+        const int n = d.spec_count[i];
+        stride = std::max(stride, (32 / node_group_width(n)) *
+                                      node_group_scratch(n, d.node_kind[i] == PIMC_NODES_FREE));
+      }
   L.nodescr_stride = (stride + 1) & ~1;
   const int need = off + nwarps * L.nodescr_stride;
   const int limit = 200 * 1024 / 8;
@@ -332,8 +366,9 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
 }
 
 void set_smem_caps() {
-  cudaFuncSetAttribute(section_moves_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       200 * 1024);
+  section_smem_cap_v2(200 * 1024);
+  section_smem_cap_v3(200 * 1024);
+  section_smem_cap_v4(200 * 1024);
   cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        200 * 1024);
@@ -495,8 +530,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   // shared by all engines of the process).
   set_smem_caps();
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, e->block,
-                                                e->lay.total * 8);
+  occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
   occ = std::max(occ, 1);
   e->grid = std::min(nrep, nsm * occ);
   if (!e->lay.nodescr_in_smem) {
@@ -685,9 +719,8 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
   RunParams P;
   fill_run_params(e, P, nattempt, d_rec);
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->stream>>>(P);
+  CU(section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->stream, P));
   e->launches++;
-  CU(cudaGetLastError());
   if (records) {
     CU(cudaMemcpyAsync(records, d_rec, sizeof(pimc_move_record) * (size_t)e->nrep * nattempt,
                        cudaMemcpyDeviceToHost, e->stream));
@@ -756,7 +789,7 @@ int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy
         RunParams P;
         fill_run_params(e, P, nattempt, nullptr);
         cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->cap_stream);
-        section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->cap_stream>>>(P);
+        section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->cap_stream, P);
       }
       rc = enqueue_thermo(e, e->cap_stream, k);
     }
@@ -917,13 +950,14 @@ int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
 
 // ------------------------------------------------- launch configuration
 namespace {
-int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap) {
+int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int minb) {
   if (block != 64 && block != 128 && block != 256) return fail(PIMC_ERR_INVALID, "block must be 64, 128 or 256");
+  if (minb < 2 || minb > 4) return fail(PIMC_ERR_INVALID, "register variant must be 2, 3 or 4");
   bool ok = false;
   const Layout L = make_layout(e->hsys, block / 32, ok, opts);
   if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, block, L.total * 8);
+  occ = section_occupancy(minb, block, L.total * 8);
   occ = std::max(occ, 1);
   if (ctas_cap > 0) occ = std::min(occ, ctas_cap);
   const int grid = std::min(e->nrep, e->num_sms * occ);
@@ -937,6 +971,7 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap) {
   e->lay = L;
   e->lay_opts = opts;
   e->ctas_cap = ctas_cap;
+  e->minb = minb;
   e->block = block;
   e->grid = grid;
   if (e->graph) {  // captured with the old launch shape
@@ -951,7 +986,7 @@ int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg) {
   if (!e || e->server || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
   LayoutOpts o;
   o.scratch_global = cfg->scratch_global != 0;
-  return apply_config(e, cfg->block, o, cfg->ctas_per_sm);
+  return apply_config(e, cfg->block, o, cfg->ctas_per_sm, cfg->regs_variant ? cfg->regs_variant : 2);
 }
 
 int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg) {
@@ -959,6 +994,7 @@ int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg) {
   cfg->block = e->block;
   cfg->scratch_global = e->lay.nodescr_in_smem ? 0 : 1;
   cfg->ctas_per_sm = e->ctas_cap;
+  cfg->regs_variant = e->minb;
   cfg->ms = 0.f;
   return PIMC_OK;
 }
@@ -984,13 +1020,14 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   };
   if (int rc = copy(true)) return rc;
   const long long launches0 = e->launches;
-  const int blk0 = e->block, cap0 = e->ctas_cap;
+  const int blk0 = e->block, cap0 = e->ctas_cap, minb0 = e->minb;
   const LayoutOpts opt0 = e->lay_opts;
   bool fixed = false;
   for (const DevSys& d : e->hsys) fixed |= d.fixed_node != 0;
   std::vector<pimc_launch_config> cand;
-  for (int b : {64, 128, 256})
-    for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({b, g, 0, 0.f});
+  for (int v : {2, 3, 4})
+    for (int b : {64, 128, 256})
+      for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
   cudaEvent_t t0, t1;
   CU(cudaEventCreate(&t0));
   CU(cudaEventCreate(&t1));
@@ -998,7 +1035,7 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   for (pimc_launch_config& c : cand) {
     LayoutOpts o;
     o.scratch_global = c.scratch_global != 0;
-    if (apply_config(e, c.block, o, c.ctas_per_sm) != PIMC_OK) {
+    if (apply_config(e, c.block, o, c.ctas_per_sm, c.regs_variant) != PIMC_OK) {
       c.ms = -1.f;  // does not fit
       continue;
     }
@@ -1027,10 +1064,10 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   if (ibest >= 0) {
     LayoutOpts o;
     o.scratch_global = cand[ibest].scratch_global != 0;
-    rc = apply_config(e, cand[ibest].block, o, cand[ibest].ctas_per_sm);
+    rc = apply_config(e, cand[ibest].block, o, cand[ibest].ctas_per_sm, cand[ibest].regs_variant);
     *best = cand[ibest];
   } else {
-    rc = apply_config(e, blk0, opt0, cap0);
+    rc = apply_config(e, blk0, opt0, cap0, minb0);
     pimc_engine_get_config(e, best);
   }
   if (int rc2 = copy(false)) return rc2;
@@ -1094,8 +1131,7 @@ int refresh_order(pimc_engine* e) {
     e->lay = make_layout(live, e->block / 32, ok);
     if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
     int occ = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, section_moves_kernel, e->block,
-                                                  e->lay.total * 8);
+    occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
     e->grid = std::min(e->nactive, e->num_sms * std::max(occ, 1));
     if (!e->lay.nodescr_in_smem) {
       const size_t need = (size_t)e->grid * (e->block / 32) * e->lay.nodescr_stride;
@@ -1304,9 +1340,8 @@ int pimc_server_run(pimc_engine* e) {
   P.seed = e->seed;
   P.lay = e->lay;
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  section_moves_kernel<<<e->grid, e->block, e->lay.total * 8, e->stream>>>(P);
+  CU(section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->stream, P));
   e->launches++;
-  CU(cudaGetLastError());
   return PIMC_OK;
 }
 

@@ -1,5 +1,5 @@
-// Kernels: the section-move sampler, the thermodynamic energy estimator, and
-// the Action-/NodeModel-level entry points.
+// The section-move sampler: shared-memory layout, section staging, mover,
+// fixed-node set-up and levels, and the persistent kernel itself.
 #pragma once
 #include "../../include/pimc_gb300.h"
 #include "section_kernel.cuh"
@@ -77,7 +77,7 @@ __device__ __forceinline__ int wrap_slice(int islice, int M) {
   return islice < 0 ? islice + M : (islice < M ? islice : islice - M);
 }
 
-__device__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
+static __device__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
                              double* sy, double* sz) {
   const int np = s.npart, n = s.nsec * np;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
@@ -91,7 +91,7 @@ __device__ void load_section(const DevSys& s, const double* path, int ifirst, do
 }
 
 // SerialPaths::putBeads (src/base/SerialPaths.cc:143-185) with the identity permutation.
-__device__ void store_section(const DevSys& s, double* path, int ifirst, const double* sx,
+static __device__ void store_section(const DevSys& s, double* path, int ifirst, const double* sx,
                               const double* sy, const double* sz) {
   const int np = s.npart, n = s.nsec * np;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
@@ -109,7 +109,7 @@ __device__ void store_section(const DevSys& s, double* path, int ifirst, const d
 // FreeMover::makeMove (src/advancer/mover/FreeMover.cc:59-124) and
 // FreeMoverPBC::makeMove (src/advancer/mover/FreeMoverPBC.cc:59-152) for one
 // moving particle at one level; threads own moved slices.  Returns ln(T_old/T_new).
-__device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
+static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
                               uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
@@ -122,8 +122,18 @@ __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int lev
   for (int k = threadIdx.x; k < nmov; k += blockDim.x) {
     const int t = nStride * (2 * k + 1), tp = t - nStride, tn = t + nStride;
     double z0, z1, z2, z3;
-    stream_normal_pair(seed, rep, att, 2u * (ord0 + k), &z0, &z1);
-    stream_normal_pair(seed, rep, att, 2u * (ord0 + k) + 1u, &z2, &z3);
+    if (s.mixed) {
+      float f0, f1, f2, f3;
+      stream_normal_pair_f(seed, rep, att, 2u * (ord0 + k), &f0, &f1);
+      stream_normal_pair_f(seed, rep, att, 2u * (ord0 + k) + 1u, &f2, &f3);
+      z0 = f0;
+      z1 = f1;
+      z2 = f2;
+      z3 = f3;
+    } else {
+      stream_normal_pair(seed, rep, att, 2u * (ord0 + k), &z0, &z1);
+      stream_normal_pair(seed, rep, att, 2u * (ord0 + k) + 1u, &z2, &z3);
+    }
     const double ox = m.s1x[t * np + ipart], oy = m.s1y[t * np + ipart], oz = m.s1z[t * np + ipart];
     const double opx = m.s1x[tp * np + ipart], opy = m.s1y[tp * np + ipart], opz = m.s1z[tp * np + ipart];
     const double onx = m.s1x[tn * np + ipart], ony = m.s1y[tn * np + ipart], onz = m.s1z[tn * np + ipart];
@@ -231,7 +241,7 @@ __device__ __forceinline__ double* cache_entry(const DevSys& s, double* cache, i
 // (src/fixednode/SHONodes.cc:112-126): slices are evaluated in parallel at the
 // current scale; at the first slice whose determinant leaves [1e-50, 1e50] the
 // loop is replayed sequentially, and later slices are re-evaluated.
-__device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
+static __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
                                 int msp, uint32_t* status, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, M = s.nslice;
@@ -375,7 +385,7 @@ __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, i
 
 // FixedNodeAction::getActionDifference (src/fixednode/FixedNodeAction.cc:39-131)
 // for the moving species at one level.
-__device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
+static __device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
                              int level, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max;
@@ -448,7 +458,11 @@ __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int leve
   return u;
 }
 
-__global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
+// MINB sets the register budget (65536 / (kBlock * MINB) per thread); the
+// variants are compiled in separate translation units (section_variants.cu)
+// and chosen at run time by the launch configuration.
+template <int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) section_moves_kernel(RunParams P) {
   extern __shared__ double smem[];
   __shared__ DevSys S;
   __shared__ double scale[kMaxSpecies];
@@ -630,462 +644,6 @@ __global__ void __launch_bounds__(kBlock) section_moves_kernel(RunParams P) {
       }
     }
     __syncthreads();
-  }
-}
-
-// ------------------------------------------------------------------ estimator
-// utau of one link (ipart, islice) summed over the composite action, as
-// CompositeAction::getBeadAction feeds ThermoEnergyEstimator::handleLink:
-// SpringAction (src/action/SpringAction.cc:112-123), SHOAction
-// (src/action/SHOAction.cc:71-105), PrimSHOAction (src/action/PrimSHOAction.cc:66-81),
-// PairAction (src/action/PairAction.cc:509-599).  The Ewald term is added per slice.
-__device__ double link_utau(const DevSys& s, const double* path, int ip, int t,
-                            bool with_pairs = true) {
-  const int np = s.npart, M = s.nslice;
-  const int tm = t == 0 ? M - 1 : t - 1;
-  const double* b1 = path + ((size_t)t * np + ip) * 3;
-  const double* b0 = path + ((size_t)tm * np + ip) * 3;
-  const int sp = species_of(s, ip);
-  const double tau = s.tau;
-  double utau = 0.0;
-  double dx = b1[0] - b0[0], dy = b1[1] - b0[1], dz = b1[2] - b0[2];
-  pbc(s, dx, dy, dz);
-  if (s.spring) utau += 3 / (2 * tau) - dot3(dx, dy, dz, dx, dy, dz) / (4.0 * s.lambda[sp] * tau * tau);
-  const double om = s.sho_omega[sp];
-  if (om > 0) {
-    const double m = s.mass[sp];
-    const double coshwt = s.sho_cosh0[sp], cschwt = s.sho_csch[sp], cothwt = s.sho_coth[sp];
-    const double tin = 1.0 / tau;
-    const double r0r0 = b0[0] * b0[0] + b0[1] * b0[1] + b0[2] * b0[2];
-    const double r1r1 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
-    const double r0r1 = b0[0] * b1[0] + b0[1] * b1[1] + b0[2] * b1[2];
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    utau += 0.5 * 3 * om * cothwt +
-            0.5 * m * om * om *
-                ((r1r1 + r0r0) * (1 - cothwt * cothwt) + 2.0 * r0r1 * coshwt * cschwt * cschwt) +
-            0.5 * m * d2 * tin * tin - 0.5 * 3 * tin;
-  }
-  if (s.prim_a[sp] != 0 || s.prim_b[sp] != 0) {
-    const double x2 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
-    utau += s.prim_a[sp] * x2 + s.prim_b[sp] * x2 * x2;
-  }
-  if (s.coulomb && with_pairs) {
-    double uc = 0.0;
-    for (int ti = 0; ti < s.ntab; ++ti) {
-      const DevTable& tb = s.tab[ti];
-      int jb, je;
-      if (ip >= tb.ifirst1 && ip < tb.ifirst1 + tb.npart1) {
-        jb = tb.ifirst2;
-        je = tb.ifirst2 + tb.npart2;
-      } else if (ip >= tb.ifirst2 && ip < tb.ifirst2 + tb.npart2) {
-        jb = tb.ifirst1;
-        je = tb.ifirst1 + tb.npart1;
-      } else {
-        continue;
-      }
-      double up = 0.0;
-      for (int j = jb; j < je; ++j) {
-        if (j == ip) continue;
-        const double* c1 = path + ((size_t)t * np + j) * 3;
-        const double* c0 = path + ((size_t)tm * np + j) * 3;
-        double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
-        pbc(s, ex, ey, ez);
-        double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
-        pbc(s, px, py, pz);
-        if (s.mixed) {
-          const float fx = (float)ex, fy = (float)ey, fz = (float)ez;
-          const float gx = (float)px, gy = (float)py, gz = (float)pz;
-          const float r = sqrtf(fx * fx + fy * fy + fz * fz);
-          const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
-          const float q = 0.5f * (r + rp);
-          const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
-          const float s2 = __fdividef(sx * sx + sy * sy + sz * sz, q * q);
-          up += 0.5 * (double)tab_uk0d_tau_f(tb, q, s2);
-          continue;
-        }
-        const double r = sqrt(dot3(ex, ey, ez, ex, ey, ez));
-        const double rp = sqrt(dot3(px, py, pz, px, py, pz));
-        const double q = 0.5 * (r + rp);
-        const double sx = ex - px, sy = ey - py, sz = ez - pz;
-        const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (q * q);
-        double v, vt;
-        tab_uk0d(tb, q, s2, v, vt);
-        up += 0.5 * vt;
-      }
-      uc += up;
-    }
-    utau += uc;
-  }
-  return utau;
-}
-
-struct ThermoParams {
-  const DevSys* sys;
-  const int* index;  // replicas to measure (null: all, blockIdx.y)
-  const double* paths;
-  double* partial;  // [nrep][nchunk]
-  int nchunk;
-  int nrep;
-  Layout lay;
-};
-
-// True when the minimum image of -v is not the negative of v's (a component
-// exactly at half a box length, where the image rounding breaks the tie
-// one way): the pair term then differs between the two orderings.
-__device__ __forceinline__ bool pbc_tie(const DevSys& s, double x, double y, double z) {
-  if (!(dot3(x, y, z, x, y, z) > s.rcut2)) return false;
-  const double v[3] = {x, y, z};
-  for (int d = 0; d < 3; ++d) {
-    const double ip = floor(__dadd_rn(__dmul_rn(s.cellb[d], v[d]), 1000.5)) - 1000;
-    const double im = floor(__dadd_rn(__dmul_rn(s.cellb[d], -v[d]), 1000.5)) - 1000;
-    if (im != -ip) return true;
-  }
-  return false;
-}
-
-// utau of the ordered pair (i, j) on the link ending at slice t (PairAction's
-// derivative term of the Coulomb pair action, src/action/PairAction.cc:509-599).
-__device__ double pair_utau_ordered(const DevSys& s, const DevTable& tb, const double* path, int i,
-                                    int j, int t) {
-  const int np = s.npart, M = s.nslice;
-  const int tm = t == 0 ? M - 1 : t - 1;
-  const double* b1 = path + ((size_t)t * np + i) * 3;
-  const double* b0 = path + ((size_t)tm * np + i) * 3;
-  const double* c1 = path + ((size_t)t * np + j) * 3;
-  const double* c0 = path + ((size_t)tm * np + j) * 3;
-  double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
-  pbc(s, ex, ey, ez);
-  double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
-  pbc(s, px, py, pz);
-  if (s.mixed) {
-    const float fx = (float)ex, fy = (float)ey, fz = (float)ez;
-    const float gx = (float)px, gy = (float)py, gz = (float)pz;
-    const float r = sqrtf(fx * fx + fy * fy + fz * fz);
-    const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
-    const float q = 0.5f * (r + rp);
-    const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
-    const float s2 = __fdividef(sx * sx + sy * sy + sz * sz, q * q);
-    return (double)tab_uk0d_tau_f(tb, q, s2);
-  }
-  const double r = sqrt(dot3(ex, ey, ez, ex, ey, ez));
-  const double rp = sqrt(dot3(px, py, pz, px, py, pz));
-  const double q = 0.5 * (r + rp);
-  const double sx = ex - px, sy = ey - py, sz = ez - pz;
-  const double s2 = dot3(sx, sy, sz, sx, sy, sz) / (q * q);
-  double v, vt;
-  tab_uk0d(tb, q, s2, v, vt);
-  return vt;
-}
-
-// The pair's share of Σ_links utau: pi-qmc adds 0.5 utau for each ordering
-// (PairAction::getBeadAction runs over every partner of every particle); the two
-// orderings agree unless an image tie makes them differ, so one evaluation
-// usually stands for both.
-__device__ double pair_utau(const DevSys& s, const DevTable& tb, const double* path, int i, int j,
-                            int t) {
-  const int np = s.npart, M = s.nslice;
-  const int tm = t == 0 ? M - 1 : t - 1;
-  const double* b1 = path + ((size_t)t * np + i) * 3;
-  const double* b0 = path + ((size_t)tm * np + i) * 3;
-  const double* c1 = path + ((size_t)t * np + j) * 3;
-  const double* c0 = path + ((size_t)tm * np + j) * 3;
-  const bool tie = pbc_tie(s, b1[0] - c1[0], b1[1] - c1[1], b1[2] - c1[2]) ||
-                   pbc_tie(s, b0[0] - c0[0], b0[1] - c0[1], b0[2] - c0[2]);
-  const double a = pair_utau_ordered(s, tb, path, i, j, t);
-  if (!tie) return a;
-  return 0.5 * a + 0.5 * pair_utau_ordered(s, tb, path, j, i, t);
-}
-
-// Pair k of round rd of the round-robin schedule over n (even) players: every
-// round pairs all players once, so a flat (round, k) index covers each
-// unordered pair exactly once without a triangular index.
-__device__ __forceinline__ void round_robin_pair(int n, int rd, int k, int& a, int& b) {
-  const int m = n - 1;
-  if (k == 0) {
-    a = m;
-    b = rd;
-  } else {
-    a = (rd + k) % m;
-    b = (rd - k + m) % m;
-  }
-}
-
-// Per-replica energy from the chunk partials: chunks summed in order, then
-// divided by the slice count (ThermoEnergyEstimator's normalisation).
-__global__ void thermo_reduce_kernel(const DevSys* sys, const int* index, const double* partial,
-                                     int nchunk, int nrow, double* energy) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nrow) return;
-  const int r = index ? index[k] : k;
-  double s = 0.0;
-  for (int c = 0; c < nchunk; ++c) s = __dadd_rn(s, partial[(size_t)k * nchunk + c]);
-  energy[r] = __ddiv_rn(s, (double)sys[r].nslice);
-}
-
-// One CTA per (chunk of slices, replica): link utau sums plus, for Coulomb with
-// Ewald, the long-range energy of each slice (CoulombAction::getBeadAction adds
-// it at ipart == 0, src/action/CoulombAction.cc:165-171).
-__global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
-  extern __shared__ double smem[];
-  __shared__ DevSys S;
-  const int r = P.index ? P.index[blockIdx.y] : blockIdx.y;
-  {
-    const int* src = (const int*)(P.sys + r);
-    int* dst = (int*)&S;
-    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
-      dst[i] = src[i];
-  }
-  __syncthreads();
-  const DevSys& s = S;
-  const double* path = P.paths + s.path_offset;
-  const int M = s.nslice, np = s.npart;
-  const int per = (M + P.nchunk - 1) / P.nchunk;
-  const int t0 = blockIdx.x * per, t1 = min(M, t0 + per);
-  Smem m = carve(smem, P.lay, s, nullptr);
-  // table of each species pair (pairs with no table contribute nothing)
-  __shared__ signed char tabof[kMaxSpecies][kMaxSpecies];
-  if (threadIdx.x < kMaxSpecies * kMaxSpecies) {
-    const int a = threadIdx.x / kMaxSpecies, b = threadIdx.x % kMaxSpecies;
-    int ti = -1;
-    for (int k = 0; k < s.ntab; ++k)
-      if ((s.tab[k].s1 == a && s.tab[k].s2 == b) || (s.tab[k].s1 == b && s.tab[k].s2 == a)) ti = k;
-    tabof[a][b] = (signed char)ti;
-  }
-  __syncthreads();
-  double part = 0.0;
-  for (int it = threadIdx.x; it < (t1 - t0) * np; it += blockDim.x) {
-    const int t = t0 + it / np, ip = it % np;
-    part += link_utau(s, path, ip, t, false);
-  }
-  if (s.coulomb && np > 1) {
-    // every pair once per slice: rounds of the round-robin schedule (np rounded up to even)
-    const int ne = np + (np & 1), per_round = ne / 2, nrd = ne - 1;
-    const int items = (t1 - t0) * nrd * per_round;
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
-      const int t = t0 + it / (nrd * per_round);
-      const int rest = it % (nrd * per_round);
-      int a, b;
-      round_robin_pair(ne, rest / per_round, rest % per_round, a, b);
-      if (a >= np || b >= np) continue;  // the bye of an odd count
-      const int ti = tabof[species_of(s, a)][species_of(s, b)];
-      if (ti < 0) continue;
-      part += pair_utau(s, s.tab[ti], path, a, b, t);
-    }
-  }
-  double tot = block_sum(part, m.red);
-  if (s.coulomb && s.ewald) {
-    for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
-    for (int t = t0; t < t1; ++t) {
-      __syncthreads();
-      for (int i = threadIdx.x; i < np; i += blockDim.x) {
-        const double* b = path + ((size_t)t * np + i) * 3;
-        m.s1x[i] = b[0];
-        m.s1y[i] = b[1];
-        m.s1z[i] = b[2];
-      }
-      if (threadIdx.x == 0) {
-        m.mx[0] = m.s1x[0];
-        m.my[0] = m.s1y[0];
-        m.mz[0] = m.s1z[0];
-      }
-      __syncthreads();
-      // ipart = 0 with the moved bead equal to the old one: new sum == old sum.
-      const double d = ewald_slice_energy(s, m, 0);
-      tot += d / s.epsilon;
-    }
-  }
-  if (threadIdx.x == 0) P.partial[(size_t)blockIdx.y * P.nchunk + blockIdx.x] = tot;
-}
-
-// ------------------------------------------------------- Action-level entry
-struct ActionDiffParams {
-  const DevSys* sys;
-  const double* section;  // [nbatch][nsec][npart][3]
-  const double* moving;   // [nbatch][nsec][3]
-  const int* ipart;
-  double* ds;
-  int level;
-  Layout lay;
-};
-
-__global__ void __launch_bounds__(kBlock) action_diff_kernel(ActionDiffParams P) {
-  extern __shared__ double smem[];
-  __shared__ DevSys S;
-  {
-    const int* src = (const int*)(P.sys);
-    int* dst = (int*)&S;
-    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
-      dst[i] = src[i];
-  }
-  __syncthreads();
-  const DevSys& s = S;
-  Smem m = carve(smem, P.lay, s, nullptr);
-  const int b = blockIdx.x, np = s.npart, nsec = s.nsec;
-  const double* sec = P.section + (size_t)b * nsec * np * 3;
-  const double* mov = P.moving + (size_t)b * nsec * 3;
-  for (int idx = threadIdx.x; idx < nsec * np; idx += blockDim.x) {
-    m.s1x[idx] = sec[idx * 3];
-    m.s1y[idx] = sec[idx * 3 + 1];
-    m.s1z[idx] = sec[idx * 3 + 2];
-  }
-  for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
-    m.mx[t] = mov[t * 3];
-    m.my[t] = mov[t * 3 + 1];
-    m.mz[t] = mov[t * 3 + 2];
-  }
-  for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
-  __syncthreads();
-  const int ip = P.ipart[b];
-  double ds = block_sum(action_partial(s, m, ip, P.level), m.red);
-  if (s.ewald && s.coulomb && P.level == 0)
-    for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ip, t);
-  if (threadIdx.x == 0) P.ds[b] = ds;
-}
-
-// ---------------------------------------------------- NodeModel-level entry
-struct NodeEvalParams {
-  const DevSys* sys;
-  const DevState* state;
-  const double* r1;  // [nbatch][npart][3]
-  const double* r2;
-  double* det;
-  double* d1;  // [nbatch][npart]
-  double* d2;
-  int* err;
-  int ispec;
-  Layout lay;
-};
-
-__global__ void __launch_bounds__(kBlock) node_eval_kernel(NodeEvalParams P) {
-  extern __shared__ double smem[];
-  __shared__ DevSys S;
-  {
-    const int* src = (const int*)(P.sys);
-    int* dst = (int*)&S;
-    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
-      dst[i] = src[i];
-  }
-  __syncthreads();
-  const DevSys& s = S;
-  const int np = s.npart, b = blockIdx.x, sp = P.ispec;
-  double* sx = smem;
-  double* sy = sx + 2 * np;
-  double* sz = sy + 2 * np;
-  double* dd = sz + 2 * np;  // [2][np]
-  double* scr = dd + 2 * np;
-  for (int i = threadIdx.x; i < np; i += blockDim.x) {
-    sx[i] = P.r1[((size_t)b * np + i) * 3];
-    sy[i] = P.r1[((size_t)b * np + i) * 3 + 1];
-    sz[i] = P.r1[((size_t)b * np + i) * 3 + 2];
-    sx[np + i] = P.r2[((size_t)b * np + i) * 3];
-    sy[np + i] = P.r2[((size_t)b * np + i) * 3 + 1];
-    sz[np + i] = P.r2[((size_t)b * np + i) * 3 + 2];
-    dd[i] = 200;
-    dd[np + i] = 200;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    SliceView v1{sx, sy, sz, np, 0, -1, 0, 0, 0};
-    SliceView v2{sx, sy, sz, np, 1, -1, 0, 0, 0};
-    double det;
-    int err;
-    const int f = s.spec_first[sp];
-    node_eval_warp(s, sp, v1, v2, P.state[0].node_scale[sp], scr, 1, det, err, dd + f, dd + np + f);
-    if (threadIdx.x == 0) {
-      P.det[b] = det;
-      P.err[b] = err;
-    }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < np; i += blockDim.x) {
-    P.d1[(size_t)b * np + i] = dd[i];
-    P.d2[(size_t)b * np + i] = dd[np + i];
-  }
-}
-
-// FP64 FMA throughput probe: each thread runs independent FMA chains.
-__global__ void fp64_probe_kernel(double* out, int iters) {
-  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
-  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
-  const double b = 0.999999999, c = 1e-12;
-  for (int i = 0; i < iters; ++i) {
-    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
-    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
-  }
-  if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5) out[0] = a0;
-}
-
-__global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, int n, double* u,
-                                     double* z) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  u[i] = stream_uniform(seed, rep, att, (uint32_t)i);
-  z[i] = stream_normal(seed, rep, att, (uint32_t)i);
-}
-
-}  // namespace pimc
-
-namespace pimc {
-
-// ------------------------------------------- allocation-free node evaluation
-// Scratch for node_eval_noalloc_kernel: one slot of 6 * 32 * 32 + 33 doubles
-// (rounded up to 6208: the LU, inverse and exp matrices, pivot reciprocals and
-// the three gradient matrices of free-particle nodes, for one Slater matrix of
-// up to 32 particles) per resident warp, kNoAllocSlots slots: 6.1 MiB, held by
-// every GPU that loads the library until exit.
-constexpr int kNoAllocSlots = 128;
-constexpr int kNoAllocSlot = (node_group_scratch(kMaxNs) + 31) / 32 * 32;
-__device__ __align__(256) double g_noalloc_scratch[kNoAllocSlots * kNoAllocSlot];
-
-struct NoAllocParams {
-  DevSys sys;  // by value: nothing to allocate
-  const double* r1;
-  const double* r2;
-  double* det;
-  double* d1;
-  double* d2;
-  int* err;
-  double scale;
-  int ispec;
-  int nbatch;
-  double* scratch;  // device address of g_noalloc_scratch
-};
-
-// One warp per block; block b takes batch entries b, b + gridDim.x, ... and
-// uses scratch slot b.  Positions are staged in dynamic shared memory
-// (6 * npart doubles), which is part of the launch, not an allocation.
-__global__ void __launch_bounds__(32) node_eval_noalloc_kernel(NoAllocParams P) {
-  extern __shared__ double sh[];
-  const DevSys& s = P.sys;
-  const int np = s.npart, sp = P.ispec;
-  double* sx = sh;
-  double* sy = sx + 2 * np;
-  double* sz = sy + 2 * np;
-  double* scr = P.scratch + (size_t)blockIdx.x * kNoAllocSlot;
-  const int f = s.spec_first[sp];
-  for (int b = blockIdx.x; b < P.nbatch; b += gridDim.x) {
-    for (int i = threadIdx.x; i < np; i += 32) {
-      sx[i] = P.r1[((size_t)b * np + i) * 3];
-      sy[i] = P.r1[((size_t)b * np + i) * 3 + 1];
-      sz[i] = P.r1[((size_t)b * np + i) * 3 + 2];
-      sx[np + i] = P.r2[((size_t)b * np + i) * 3];
-      sy[np + i] = P.r2[((size_t)b * np + i) * 3 + 1];
-      sz[np + i] = P.r2[((size_t)b * np + i) * 3 + 2];
-      P.d1[(size_t)b * np + i] = 200;
-      P.d2[(size_t)b * np + i] = 200;
-    }
-    __syncwarp();
-    SliceView v1{sx, sy, sz, np, 0, -1, 0, 0, 0};
-    SliceView v2{sx, sy, sz, np, 1, -1, 0, 0, 0};
-    double det;
-    int err;
-    node_eval_warp(s, sp, v1, v2, P.scale, scr, 1, det, err, P.d1 + (size_t)b * np + f,
-                   P.d2 + (size_t)b * np + f);
-    if (threadIdx.x == 0) {
-      P.det[b] = det;
-      P.err[b] = err;
-    }
-    __syncwarp();
   }
 }
 

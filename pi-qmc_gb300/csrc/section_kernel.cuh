@@ -82,7 +82,7 @@ struct SliceView {
 // jcol < 0 fills it, jcol >= 0 reuses it and recomputes column jcol only (the
 // other columns' inputs are unchanged, so the values are bit-identical).
 template <int W>
-__device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
+static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
                                 int& err_out, double* d1, double* d2,
@@ -248,20 +248,51 @@ __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
     else if (pos == pj)
       pos = j;
   }
-  if (info == 0 && gl < n) {
-    double* x = X + gl * n;
-    for (int i = 0; i < n; ++i) x[i] = (i == pos) ? 1.0 : 0.0;
-    for (int j = pos; j < n; ++j) {
-      const double xj = x[j];
-      for (int i = j + 1; i < n; ++i) x[i] -= A[j * n + i] * xj;
-    }
-    for (int j = n - 1; j >= 0; --j) {
-      const double xj = x[j] * R[j];
-      x[j] = xj;
-      for (int i = 0; i < j; ++i) x[i] -= A[j * n + i] * xj;
-    }
-  }
+  // Column c of X starts as e_pos(c); the substitutions then run one element
+  // (column, row) per lane and step.  Every element receives the same FMAs in
+  // the same order as a per-column solve (the steps before pos(c) subtract
+  // exact zeros), so the result is that solve's, bit for bit.
+  const bool inv_ok = info == 0;
+  if (inv_ok && gl < n)
+    for (int i = 0; i < n; ++i) X[gl * n + i] = (i == pos) ? 1.0 : 0.0;
   __syncwarp();
+  for (int j = 0; j < n - 1; ++j) {  // forward: x(i) -= l(i,j) x(j), i > j
+    const int m = n - j - 1;
+    if (inv_ok) {
+      int c = gl / m, ii = gl - c * m;
+      const int dc = W / m, di = W - dc * m;
+      for (int e = gl; e < n * m; e += W) {
+        const int i = j + 1 + ii;
+        X[c * n + i] -= A[j * n + i] * X[c * n + j];
+        ii += di;
+        c += dc;
+        if (ii >= m) {
+          ii -= m;
+          ++c;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  for (int j = n - 1; j >= 0; --j) {  // back: x(j) *= 1/u(j,j); x(i) -= u(i,j) x(j), i < j
+    if (inv_ok)
+      for (int c = gl; c < n; c += W) X[c * n + j] *= R[j];
+    __syncwarp();
+    if (inv_ok && j > 0) {
+      int c = gl / j, ii = gl - c * j;
+      const int dc = W / j, di = W - dc * j;
+      for (int e = gl; e < n * j; e += W) {
+        X[c * n + ii] -= A[j * n + ii] * X[c * n + j];
+        ii += di;
+        c += dc;
+        if (ii >= j) {
+          ii -= j;
+          ++c;
+        }
+      }
+    }
+    __syncwarp();
+  }
   // --- nodal distances: d = sqrt(2m / (tau |grad ln det|^2)), the gradient
   // with respect to r1_j (d1) and r2_i (d2); inv(j,i) = X[i*n + j].  (No early
   // exit: a singular group simply skips them, so the warp stays converged.)
@@ -371,7 +402,7 @@ __host__ __device__ __forceinline__ int node_group_width(int n) {
 }
 
 // One warp evaluates one slice pair (the entry-point kernels).
-__device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, const SliceView& v2,
+static __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, const SliceView& v2,
                                double scale, double* scr, int full, double& det_out,
                                int& err_out, double* d1, double* d2) {
   node_eval_group<32>(s, sp, v1, v2, scale, scr, full, nullptr, -1, true, det_out, err_out, d1,
@@ -385,7 +416,7 @@ __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& v1, con
 // (src/action/PrimSHOAction.cc:21-58), PairAction per species pair
 // (src/action/PairAction.cc:219-360).  Work items are links and (partner, link)
 // pairs; each item contributes (new - old).
-__device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level) {
+static __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
   const int nlinks = 1 << (L - level);
@@ -549,7 +580,7 @@ __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int 
 // new configuration of one slice (the new one has particle ipart at the moving
 // bead), as CoulombAction::getActionDifference uses them at level 0
 // (src/action/CoulombAction.cc:107-119).  Returns both evalLongRange values.
-__device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipart, int t, double& eold,
+static __device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipart, int t, double& eold,
                                  double& enew) {
   const int np = s.npart;
   const int kx0 = s.ikmax[0], ky0 = s.ikmax[1], kz0 = s.ikmax[2];
@@ -651,14 +682,14 @@ __device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipart, int 
 }
 
 // (new - old) * tau / epsilon of one slice, the level-0 Ewald term.
-__device__ double ewald_slice_diff(const DevSys& s, const Smem& m, int ipart, int t) {
+static __device__ double ewald_slice_diff(const DevSys& s, const Smem& m, int ipart, int t) {
   double eold, enew;
   ewald_slice_sums(s, m, ipart, t, eold, enew);
   return -(eold * s.tau / s.epsilon) + enew * s.tau / s.epsilon;
 }
 
 // evalLongRange of section slice t as staged in shared memory.
-__device__ double ewald_slice_energy(const DevSys& s, const Smem& m, int t) {
+static __device__ double ewald_slice_energy(const DevSys& s, const Smem& m, int t) {
   double eold, enew;
   ewald_slice_sums(s, m, -1, t, eold, enew);
   return eold;

@@ -54,11 +54,12 @@ class EwaldTable(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("block", C.c_int), ("scratch_global", C.c_int), ("ctas_per_sm", C.c_int),
-                ("ms", C.c_float)]
+                ("regs_variant", C.c_int), ("ms", C.c_float)]
 
     def as_dict(self):
         return {"block": self.block, "scratch_global": self.scratch_global,
-                "ctas_per_sm": self.ctas_per_sm, "ms": round(float(self.ms), 4)}
+                "ctas_per_sm": self.ctas_per_sm, "regs_variant": self.regs_variant,
+                "ms": round(float(self.ms), 4)}
 
 
 class ServerConfig(C.Structure):
@@ -338,14 +339,14 @@ class Engine:
         replica (the chains are restored), applies the fastest; returns it and
         every candidate with its time (ms < 0: does not fit)."""
         best = LaunchConfig()
-        tried = (LaunchConfig * 16)()
+        tried = (LaunchConfig * 32)()
         nt = C.c_int(0)
-        _check(lib().pimc_engine_autotune(self.h, nattempt, C.byref(best), tried, 16,
+        _check(lib().pimc_engine_autotune(self.h, nattempt, C.byref(best), tried, 32,
                                           C.byref(nt)))
-        return best.as_dict(), [tried[i].as_dict() for i in range(min(nt.value, 16))]
+        return best.as_dict(), [tried[i].as_dict() for i in range(min(nt.value, 32))]
 
-    def configure(self, block, scratch_global=0, ctas_per_sm=0):
-        cfg = LaunchConfig(block, scratch_global, ctas_per_sm, 0.0)
+    def configure(self, block, scratch_global=0, ctas_per_sm=0, regs_variant=2):
+        cfg = LaunchConfig(block, scratch_global, ctas_per_sm, regs_variant, 0.0)
         _check(lib().pimc_engine_configure(self.h, C.byref(cfg)))
 
     def launch_config(self):

@@ -11,7 +11,10 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 LIB = os.path.join(PKG, "libpimc_gb300.so")
-SOURCES = ["engine.cu", "tables.cc"]
+# (source, extra flags): the section kernel's register-budget variants are
+# separate objects so that nvcc compiles them in parallel
+SOURCES = [("engine.cu", []), ("tables.cc", [])] + [
+    ("section_variants.cu", [f"-DPIMC_MINB={v}"]) for v in (2, 3, 4)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,14 +41,15 @@ def build(force=False, verbose=False):
         return LIB
     objs = []
     procs = []
-    for src in SOURCES:
+    for src, flags in SOURCES:
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue
-        obj = os.path.join(PKG, "_build_" + src.replace(".", "_") + ".o")
+        tag = "".join(f.split("=")[-1] for f in flags)
+        obj = os.path.join(PKG, "_build_" + src.replace(".", "_") + tag + ".o")
         if src.endswith(".cu"):
             cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-Xcompiler", "-ffp-contract=off", "-c", path, "-o", obj]
+                   "-Xcompiler", "-ffp-contract=off", *flags, "-c", path, "-o", obj]
         else:
             cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", path,
                    "-o", obj]

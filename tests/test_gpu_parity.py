@@ -233,14 +233,15 @@ def test_graph_steps_equal_direct_calls(pimc):
 
 
 @pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small"])
-@pytest.mark.parametrize("block,scratch_global", [(64, 0), (128, 1), (256, 1)])
-def test_launch_configs_match_golden(pimc, case, block, scratch_global):
+@pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 4), (128, 1, 3), (256, 1, 2),
+                                                       (256, 0, 3)])
+def test_launch_configs_match_golden(pimc, case, block, scratch_global, regs):
     # Every launch configuration the autotuner may pick reproduces pi-qmc's
     # decisions and action differences.
     g = golden_io.load(case)
     e = engine_for(pimc, g)
     fixed = any(g["kw"].get("node_kind", [0]))
-    e.configure(block, scratch_global if fixed else 0)
+    e.configure(block, scratch_global if fixed else 0, 0, regs)
     e.upload_paths([g["path0"]])
     n = min(g["nattempt"], 200)
     rec = e.run_sections(n, records=True)
@@ -264,10 +265,26 @@ def test_autotune_does_not_advance_chains(pimc):
     acc, att, st = a.replica_status()
     assert att.sum() == 0
     assert a.launch_config()["block"] == best["block"]
-    b.configure(best["block"], best["scratch_global"], best["ctas_per_sm"])
+    b.configure(best["block"], best["scratch_global"], best["ctas_per_sm"], best["regs_variant"])
     ra = a.run_sections(40, records=True)
     rb = b.run_sections(40, records=True)
     assert np.array_equal(ra["reject_level"], rb["reject_level"])
     assert np.array_equal(ra["ds"], rb["ds"])
     for pa, pb in zip(a.download_paths(), b.download_paths()):
         assert np.array_equal(pa, pb)
+
+
+def test_register_variants_bit_identical(pimc):
+    # The register-budget variants compile the same arithmetic: same block size,
+    # same results bit for bit.
+    g = golden_io.load("dot4_fn")
+    out = []
+    for regs in (2, 3, 4):
+        e = engine_for(pimc, g, nreplica=4)
+        e.configure(256, 0, 0, regs)
+        e.upload_paths([g["path0"]] * 4)
+        r = e.run_sections(60, records=True)
+        out.append((r["ds"], r["ds_node"], r["reject_level"], e.download_paths(flat=True)))
+    for o in out[1:]:
+        for x, y in zip(out[0], o):
+            assert np.array_equal(x, y)
