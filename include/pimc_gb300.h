@@ -179,6 +179,25 @@ int pimc_replica_status(pimc_engine* e, int64_t* accepted, int64_t* attempted,
  * with the ThermoEnergyEstimator as the measurement. */
 int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy);
 
+/* ---- further estimators ------------------------------------------------- */
+
+/* Virial energy estimator with window nwindow (VirialEnergyEstimator,
+ * src/estimator/VirialEnergyEstimator.cc:34-79) of every replica, FP64.
+ * nwindow = 1 gives the thermodynamic estimator's value. */
+int pimc_virial_energy(pimc_engine* e, int nwindow, double* host_energy /* nreplica */);
+/* Coulomb potential energy, direct pair sum with minimum image
+ * (CoulombEnergyEstimator, src/estimator/CoulombEnergyEstimator.cc:30-44). */
+int pimc_coulomb_energy(pimc_engine* e, double epsilon, double* host_energy);
+/* Coulomb potential energy with the estimator's own optimized Ewald sum
+ * (EwaldCoulombEstimator, src/estimator/EwaldCoulombEstimator.cc:60-140): est and
+ * vgrid (1001 doubles) from pimc_ewald_estimator_tables. */
+int pimc_ewald_coulomb_energy(pimc_engine* e, double epsilon, double rcut,
+                              const pimc_ewald_table* est, const double* vgrid,
+                              double* host_energy);
+/* Builds that Ewald table and grid for a system (host only, no GPU). */
+int pimc_ewald_estimator_tables(const pimc_system* sys, double rcut, double kcut, double epsilon,
+                                const pimc_ewald_table** est, double* vgrid);
+
 /* ---- launch configuration and autotuning -------------------------------- */
 
 /* Launch configuration of an engine's section kernel: threads per replica

@@ -36,6 +36,9 @@ SOURCES = [
     "advancer/mover/FreeMoverPBC.cc", "advancer/SimpleParticleChooser.cc",
     "advancer/SpeciesParticleChooser.cc", "advancer/ParticleChooser.cc",
     "advancer/PermutationChooser.cc", "stats/AccRejEstimator.cc",
+    "estimator/VirialEnergyEstimator.cc", "estimator/CoulombEnergyEstimator.cc",
+    "estimator/EwaldCoulombEstimator.cc", "stats/ScalarEstimator.cc",
+    "stats/SimpleScalarAccumulator.cpp",
 ]
 
 FLAGS = ["-std=gnu++98", "-O2", "-fPIC", "-w", "-ffp-contract=off", "-DHAVE_CONFIG_H"]

@@ -176,6 +176,17 @@ class RefOracle(_Base):
             L.ref_run.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(OraRecord)]
             L.ref_thermo_energy.restype = C.c_double
             L.ref_thermo_energy.argtypes = [C.c_void_p]
+            L.ref_virial_energy.restype = C.c_double
+            L.ref_virial_energy.argtypes = [C.c_void_p, C.c_int]
+            L.ref_coulomb_energy.restype = C.c_double
+            L.ref_coulomb_energy.argtypes = [C.c_void_p, C.c_double]
+            L.ref_estimator_ewald.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                              C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_int), C.POINTER(C.c_double)]
+            L.ref_ewald_coulomb_energy.restype = C.c_double
+            L.ref_ewald_coulomb_energy.argtypes = [C.c_void_p, C.c_double, C.c_double,
+                                                   C.c_double]
             L.ref_bead_action.argtypes = [C.c_void_p, C.c_int, C.c_int,
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.ref_action_diff.restype = C.c_double
@@ -210,6 +221,34 @@ class RefOracle(_Base):
         self._cfg_keep = cfg
         self.h = C.c_void_p(L.ref_create(C.byref(cfg)))
         self._get, self._set, self._run = L.ref_get_path, L.ref_set_path, L.ref_run
+
+    def virial_energy(self, nwindow=1):
+        return self.lib().ref_virial_energy(self.h, nwindow)
+
+    def coulomb_energy(self, epsilon=1.0):
+        return self.lib().ref_coulomb_energy(self.h, epsilon)
+
+    def ewald_coulomb_energy(self, epsilon, rcut, kcut):
+        return self.lib().ref_ewald_coulomb_energy(self.h, epsilon, rcut, kcut)
+
+    def estimator_ewald(self, epsilon, rcut, kcut):
+        """The estimator's own Ewald table and short-range grid."""
+        L = self.lib()
+        totk = C.c_int(0)
+        scal = (C.c_double * 2)()
+        ik = (C.c_int * 3)()
+        L.ref_estimator_ewald(self.h, rcut, kcut, epsilon, C.byref(totk), None, None, scal, ik,
+                              None)
+        n = totk.value
+        kv = np.zeros(3 * n, np.int32)
+        vk = np.zeros(n)
+        vg = np.zeros(1001)
+        L.ref_estimator_ewald(self.h, rcut, kcut, epsilon, C.byref(totk),
+                              kv.ctypes.data_as(C.POINTER(C.c_int)),
+                              vk.ctypes.data_as(C.POINTER(C.c_double)), scal, ik,
+                              vg.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(totk=n, kvec=kv.reshape(n, 3), vk=vk, one_over_2v=scal[0],
+                    self_energy=scal[1], ikmax=list(ik)), vg
 
     def thermo_energy(self):
         return self.lib().ref_thermo_energy(self.h)
@@ -309,6 +348,14 @@ class PortOracle(_Base):
             L.port_init_errors.argtypes = [C.c_void_p]
             L.port_ewald_long_range.restype = C.c_double
             L.port_ewald_long_range.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+            L.port_virial_energy.restype = C.c_double
+            L.port_virial_energy.argtypes = [C.c_void_p, C.c_int]
+            L.port_coulomb_energy.restype = C.c_double
+            L.port_coulomb_energy.argtypes = [C.c_void_p, C.c_double]
+            L.port_ewald_coulomb_energy.restype = C.c_double
+            L.port_ewald_coulomb_energy.argtypes = [C.c_void_p, C.c_double, C.c_double,
+                                                    C.POINTER(OraEwaldTable),
+                                                    C.POINTER(C.c_double)]
             cls._lib = L
         return cls._lib
 
@@ -352,6 +399,29 @@ class PortOracle(_Base):
             self.lib().port_destroy(self.h)
         except Exception:
             pass
+
+    def virial_energy(self, nwindow=1):
+        return self.lib().port_virial_energy(self.h, nwindow)
+
+    def coulomb_energy(self, epsilon=1.0):
+        return self.lib().port_coulomb_energy(self.h, epsilon)
+
+    def ewald_coulomb_energy(self, epsilon, rcut, est_ewald, vgrid):
+        """est_ewald: dict(totk, kvec, vk, one_over_2v, self_energy, ikmax) of the
+        estimator's own Ewald sum; vgrid: its 1001-point -evalFR/epsilon grid."""
+        kv = np.ascontiguousarray(est_ewald["kvec"], np.int32).ravel()
+        vk = np.ascontiguousarray(est_ewald["vk"], np.float64)
+        vg = np.ascontiguousarray(vgrid, np.float64)
+        et = OraEwaldTable()
+        et.totk = int(est_ewald["totk"])
+        et.kvec = kv.ctypes.data_as(C.POINTER(C.c_int))
+        et.vk = vk.ctypes.data_as(C.POINTER(C.c_double))
+        et.one_over_2v = float(est_ewald["one_over_2v"])
+        et.self_energy = float(est_ewald["self_energy"])
+        for d in range(3):
+            et.ikmax[d] = int(est_ewald["ikmax"][d])
+        return self.lib().port_ewald_coulomb_energy(self.h, epsilon, rcut, C.byref(et),
+                                                    vg.ctypes.data_as(C.POINTER(C.c_double)))
 
     def thermo_energy(self):
         return self.lib().port_thermo_energy(self.h)

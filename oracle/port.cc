@@ -132,6 +132,35 @@ struct PairTab {
     }
     return action;
   }
+  // uk0CalcDerivatives with the q and s^2 derivatives (src/action/PairAction.cc:641-660).
+  void uk0dd(double q, double s2, double& u, double& utau, double& uq, double& us2) const {
+    q *= rgridinv;
+    double x = log(q) * logrratioinv;
+    int i = (int)x;
+    if (q < 1) {
+      i = 0;
+      x = 0;
+    } else if (i > ngpts - 2) {
+      i = ngpts - 2;
+      x = 1;
+    } else {
+      x -= i;
+    }
+    u = utau = uq = us2 = 0;
+    for (int k = norder; k >= 0; k--) {
+      u *= s2;
+      u += (1 - x) * g(i, 0, k) + x * g(i + 1, 0, k);
+      utau *= s2;
+      utau += (1 - x) * g(i, 1, k) + x * g(i + 1, 1, k);
+      uq *= s2;
+      uq += g(i + 1, 0, k) - g(i, 0, k);
+    }
+    uq *= logrratioinv * rgridinv / q;
+    for (int k = norder; k > 0; k--) {
+      us2 *= s2;
+      us2 += k * ((1 - x) * g(i, 0, k) + x * g(i + 1, 0, k));
+    }
+  }
   void uk0d(double q, double s2, double& u, double& utau) const {
     int i;
     double x;
@@ -1020,11 +1049,199 @@ struct Sim {
       for (int ip = 0; ip < np; ++ip) sum += beadUtau(ip, islice);
     return sum / ns;
   }
+
+  // The forces fm, fp of getBeadAction summed over the actions: SpringAction
+  // (src/action/SpringAction.cc:112-123), SHOAction (SHOAction.cc:71-105),
+  // PrimSHOAction (PrimSHOAction.cc:65-81), PairAction (PairAction.cc:509-599);
+  // the Ewald long-range term and FixedNodeAction add none.
+  void beadForces(int ip, int islice, double* fm, double* fp) {
+    for (int d = 0; d < 3; ++d) fm[d] = fp[d] = 0;
+    const int sp = spec[ip];
+    const double tau = cfg.tau;
+    if (cfg.spring) {
+      double dm[3], dp[3];
+      for (int d = 0; d < 3; ++d) {
+        dm[d] = bead(ip, islice).x[d] - bead(ip, islice - 1).x[d];
+        dp[d] = bead(ip, islice).x[d] - bead(ip, islice + 1).x[d];
+      }
+      cell.pbc(dm);
+      cell.pbc(dp);
+      for (int d = 0; d < 3; ++d) {
+        fm[d] -= dm[d] / (2 * lambda[ip] * tau);
+        fp[d] -= dp[d] / (2 * lambda[ip] * tau);
+      }
+    }
+    if (cfg.sho_omega[sp] > 0) {
+      const double omega = cfg.sho_omega[sp], m = cfg.spec_mass[sp];
+      const double wt = omega * tau, sinhwt = sinh(wt), coshwt = cosh(wt);
+      const double cschwt = 1.0 / sinhwt, tin = 1.0 / tau;
+      const double* r1 = bead(ip, islice).x;
+      const double* r0 = bead(ip, islice - 1).x;
+      const double* r2 = bead(ip, islice + 1).x;
+      double dm[3], dp[3];
+      for (int d = 0; d < 3; ++d) {
+        dm[d] = r1[d] - r0[d];
+        dp[d] = r1[d] - r2[d];
+      }
+      cell.pbc(dm);
+      cell.pbc(dp);
+      for (int d = 0; d < 3; ++d) {
+        fm[d] -= m * omega * (r1[d] * coshwt - r0[d]) * cschwt - m * dm[d] * tin;
+        fp[d] -= m * omega * (r1[d] * coshwt - r2[d]) * cschwt - m * dp[d] * tin;
+      }
+    }
+    if (cfg.prim_a[sp] != 0 || cfg.prim_b[sp] != 0) {
+      const double* x = bead(ip, islice).x;
+      double x2 = 0;
+      for (int d = 0; d < 3; ++d) x2 += x[d] * x[d];
+      const double a = cfg.prim_a[sp], b = cfg.prim_b[sp];
+      for (int d = 0; d < 3; ++d) {
+        fm[d] += -0.5 * (2 * a + 4 * b * x2) * tau * x[d];
+        fp[d] += -0.5 * (2 * a + 4 * b * x2) * tau * x[d];
+      }
+    }
+    if (cfg.coulomb) {
+      for (size_t k = 0; k < pairs.size(); ++k) {
+        const PairTab& pt = pairs[k];
+        int jbegin, jend;
+        if (ip >= pt.ifirst1 && ip < pt.ifirst1 + pt.npart1) {
+          jbegin = pt.ifirst2;
+          jend = pt.ifirst2 + pt.npart2;
+        } else if (ip >= pt.ifirst2 && ip < pt.ifirst2 + pt.npart2) {
+          jbegin = pt.ifirst1;
+          jend = pt.ifirst1 + pt.npart1;
+        } else {
+          continue;
+        }
+        for (int j = jbegin; j < jend; ++j) {
+          if (ip == j) continue;
+          double delta[3], prev[3], next[3];
+          for (int d = 0; d < 3; ++d) {
+            delta[d] = bead(ip, islice).x[d] - bead(j, islice).x[d];
+            prev[d] = bead(ip, islice - 1).x[d] - bead(j, islice - 1).x[d];
+            next[d] = bead(ip, islice + 1).x[d] - bead(j, islice + 1).x[d];
+          }
+          cell.pbc(delta);
+          cell.pbc(prev);
+          cell.pbc(next);
+          const double r = sqrt(dot3(delta, delta));
+          for (int side = 0; side < 2; ++side) {
+            const double* o = side == 0 ? prev : next;
+            const double ro = sqrt(dot3(o, o));
+            const double q = 0.5 * (r + ro);
+            double sv[3] = {delta[0] - o[0], delta[1] - o[1], delta[2] - o[2]};
+            const double s2 = dot3(sv, sv) / (q * q);
+            double v, vtau, vq, vs2;
+            pt.uk0dd(q, s2, v, vtau, vq, vs2);
+            double* f = side == 0 ? fm : fp;
+            for (int d = 0; d < 3; ++d)
+              f[d] -= vq * delta[d] / (2 * r) + vs2 * (2 * sv[d] / (q * q) - s2 * delta[d] / (q * r));
+          }
+        }
+      }
+    }
+  }
+
+  // VirialEnergyEstimator::handleLink / endCalc (src/estimator/VirialEnergyEstimator.cc:34-79)
+  // over SerialPaths::sumOverLinks' order (src/base/SerialPaths.cc:48-66).
+  double virialEnergy(int nwindow) {
+    std::vector<double> r0(3 * np, 0.0), rav(3 * np, 0.0), fav(3 * np, 0.0);
+    double energy = 0;
+    const double tau = cfg.tau;
+    for (int islice = 0; islice < ns; ++islice) {
+      for (int ip = 0; ip < np; ++ip) {
+        double* R0 = &r0[3 * ip];
+        double* RAV = &rav[3 * ip];
+        double* FAV = &fav[3 * ip];
+        if (islice % nwindow == 0) {
+          energy += (1 / (2 * tau)) * dot3(FAV, R0);
+          for (int d = 0; d < 3; ++d) R0[d] = RAV[d] = FAV[d] = 0;
+        }
+        const int thisWindow = (islice / nwindow < (ns - 1) / nwindow) ? nwindow
+                                                                        : (ns - 1) % nwindow + 1;
+        double r[3];
+        for (int d = 0; d < 3; ++d) r[d] = bead(ip, islice).x[d] - bead(ip, islice - 1).x[d];
+        cell.pbc(r);
+        for (int d = 0; d < 3; ++d) {
+          RAV[d] += r[d];
+          R0[d] += (thisWindow - islice % nwindow) * r[d] / thisWindow;
+        }
+        double fm[3], fp[3];
+        beadForces(ip, islice, fm, fp);
+        const double utau = beadUtau(ip, islice);
+        double f[3];
+        for (int d = 0; d < 3; ++d) {
+          f[d] = fm[d] + fp[d];
+          FAV[d] += f[d];
+        }
+        energy += utau;
+        energy += -(1. - 1. / thisWindow) * (3 / (2 * tau)) - (1 / (2 * tau)) * dot3(f, RAV);
+      }
+    }
+    for (int ip = 0; ip < np; ++ip) energy += (1 / (2 * tau)) * dot3(&fav[3 * ip], &r0[3 * ip]);
+    return energy / ns;
+  }
+
+  // CoulombEnergyEstimator::handleLink (src/estimator/CoulombEnergyEstimator.cc:30-40).
+  double coulombEnergy(double epsilon) {
+    double e = 0;
+    for (int islice = 0; islice < ns; ++islice)
+      for (int ip = 0; ip < np; ++ip) {
+        double energy = 0;  // one link's sum, then added (ScalarAccumulator::addToValue)
+        for (int j = 0; j < ip; ++j) {
+          double d[3];
+          for (int a = 0; a < 3; ++a) d[a] = bead(ip, islice).x[a] - bead(j, islice).x[a];
+          cell.pbc(d);
+          energy += charge(ip) * charge(j) / (epsilon * sqrt(dot3(d, d)));
+        }
+        e += energy;
+      }
+    return e / ns;
+  }
+
+  // EwaldCoulombEstimator::handleLink, optimized-Ewald branch
+  // (src/estimator/EwaldCoulombEstimator.cc:102-140): tabulated short range up to
+  // rcut (pi-qmc interpolates with x = r - i dr, not divided by dr), plus the
+  // long-range sum of each slice.
+  double ewaldCoulombEnergy(double epsilon, double rcut, const Ewald& est,
+                            const std::vector<double>& vgrid) {
+    const double dr = rcut / 1000, drinv = 1. / dr;
+    double e = 0;
+    for (int islice = 0; islice < ns; ++islice)
+      for (int ip = 0; ip < np; ++ip) {
+        double energy = 0.0;
+        for (int j = 0; j < ip; ++j) {
+          double d[3];
+          for (int a = 0; a < 3; ++a) d[a] = bead(ip, islice).x[a] - bead(j, islice).x[a];
+          cell.pbc(d);
+          const double r = sqrt(dot3(d, d));
+          if (r < rcut) {
+            const int ig = (int)(r * drinv);
+            const double x = r - ig * dr;
+            energy += charge(ip) * charge(j) *
+                      (1. / (r * epsilon) + (1 - x) * vgrid[ig] + x * vgrid[ig + 1]);
+          }
+        }
+        if (ip == 0) {
+          std::vector<V3> rew(np);
+          for (int p = 0; p < np; ++p) rew[p] = P(islice, p);
+          energy += est.evalLongRange(rew) / epsilon;
+        }
+        e += energy;
+      }
+    return e / ns;
+  }
+  double charge(int ip) const { return cfg.spec_charge[spec[ip]]; }
 };
 
 }  // namespace
 
 extern "C" {
+
+double port_virial_energy(void* h, int nwindow);
+double port_coulomb_energy(void* h, double epsilon);
+double port_ewald_coulomb_energy(void* h, double epsilon, double rcut, const ora_ewald_table* est,
+                                 const double* vgrid);
 
 void* port_create(const ora_config* c, int npair_tables, const int* pair_species,
                   const ora_pair_table* tables, const ora_ewald_table* ew) {
@@ -1158,6 +1375,25 @@ int port_run(void* h, int n, uint32_t first_attempt, ora_record* recs) {
 }
 
 double port_thermo_energy(void* h) { return ((Sim*)h)->thermoEnergy(); }
+double port_virial_energy(void* h, int nwindow) { return ((Sim*)h)->virialEnergy(nwindow); }
+double port_coulomb_energy(void* h, double epsilon) { return ((Sim*)h)->coulombEnergy(epsilon); }
+double port_ewald_coulomb_energy(void* h, double epsilon, double rcut, const ora_ewald_table* est,
+                                 const double* vgrid) {
+  Sim* s = (Sim*)h;
+  Ewald E;
+  E.totk = est->totk;
+  E.kvec.assign(est->kvec, est->kvec + 3 * est->totk);
+  E.vk.assign(est->vk, est->vk + est->totk);
+  E.oneOver2V = est->one_over_2v;
+  E.selfEnergy = est->self_energy;
+  for (int d = 0; d < 3; ++d) {
+    E.ikmax[d] = est->ikmax[d];
+    E.deltak[d] = 2 * 3.14159265358979 * s->cell.b[d];
+  }
+  for (int i = 0; i < s->np; ++i) E.q.push_back(s->charge(i));
+  std::vector<double> vg(vgrid, vgrid + 1001);
+  return s->ewaldCoulombEnergy(epsilon, rcut, E, vg);
+}
 
 double port_bead_utau(void* h, int ipart, int islice) {
   return ((Sim*)h)->beadUtau(ipart, islice);

@@ -89,9 +89,18 @@ extern "C" void oracle_shim_normals(double* out, int n) {
 // Unused on the bisection path; defined so the objects link.
 #include "action/interaction/PairIntegrator.h"
 #include "stats/ReportWriters.h"
+#include "estimator/VirialEnergyEstimator.h"
+#include "estimator/CoulombEnergyEstimator.h"
+#include "estimator/EwaldCoulombEstimator.h"
+#include "stats/SimpleScalarAccumulator.h"
 void PairIntegrator::integrate(double, double) {}
 void ReportWriters::startAccRejReport(AccRejEstimator*, ScalarAccumulator*) {}
 void ReportWriters::reportAccRejStep(AccRejEstimator*, ScalarAccumulator*) {}
+void ReportWriters::startScalarReport(ScalarEstimator*, SimpleScalarAccumulator*) {}
+void ReportWriters::reportScalarStep(ScalarEstimator*, SimpleScalarAccumulator*) {}
+void ReportWriters::startScalarReport(ScalarEstimator*, PartitionedScalarAccumulator*) {}
+void ReportWriters::reportScalarStep(ScalarEstimator*, PartitionedScalarAccumulator*) {}
+
 
 // ---- recording wrappers ---------------------------------------------------
 static ora_record* g_rec = 0;
@@ -380,6 +389,35 @@ extern "C" int ref_run(void* h, int n, uint32_t first_attempt, ora_record* recs)
   return nacc;
 }
 
+// pi-qmc's own estimators over the current paths (one evaluate() each):
+// VirialEnergyEstimator (src/estimator/VirialEnergyEstimator.cc:34-79) over the
+// composite and double actions, CoulombEnergyEstimator
+// (src/estimator/CoulombEnergyEstimator.cc:30-44) and the optimized-Ewald
+// EwaldCoulombEstimator (src/estimator/EwaldCoulombEstimator.cc:60-140).
+extern "C" double ref_virial_energy(void* h, int nwindow) {
+  RefSim* s = (RefSim*)h;
+  VirialEnergyEstimator est(*s->simInfo, s->composite, s->drec ? s->dcomposite : 0, nwindow, 0,
+                            "", 1.0, 0.0);
+  est.evaluate(*s->paths);
+  return est.calcValue();
+}
+
+extern "C" double ref_coulomb_energy(void* h, double epsilon) {
+  RefSim* s = (RefSim*)h;
+  SimpleScalarAccumulator* acc = new SimpleScalarAccumulator(0);
+  CoulombEnergyEstimator est(*s->simInfo, epsilon, "", 1.0, 0.0, acc);
+  est.evaluate(*s->paths);
+  return acc->getValue();
+}
+
+extern "C" double ref_ewald_coulomb_energy(void* h, double epsilon, double rcut, double kcut) {
+  RefSim* s = (RefSim*)h;
+  SimpleScalarAccumulator* acc = new SimpleScalarAccumulator(0);
+  EwaldCoulombEstimator est(*s->simInfo, s->composite, epsilon, rcut, kcut, "", 1.0, 0.0, acc);
+  est.evaluate(*s->paths);
+  return acc->getValue();
+}
+
 extern "C" double ref_thermo_energy(void* h) {
   RefSim* s = (RefSim*)h;
   ThermoSum ts(s->composite, s->drec ? s->dcomposite : 0);
@@ -502,6 +540,36 @@ extern "C" int ref_ewald(void* h, int* totk, int* kvec, double* vk, double* scal
     for (int i = 0; i < oe->npoly; ++i) scal[2 + i] = oe->coef(i);
   }
   for (int d = 0; d < 3; ++d) ikmax[d] = e->ikmax[d];
+  return 0;
+}
+
+// The optimized Ewald sum an EwaldCoulombEstimator builds for itself
+// (src/estimator/EwaldCoulombEstimator.cc:60-90): its k-list, v_k, 1/(2V), self
+// energy and the 1001-point short-range grid vgrid(i) = -evalFR(i rcut/1000)/eps.
+extern "C" int ref_estimator_ewald(void* h, double rcut, double kcut, double epsilon, int* totk,
+                                   int* kvec, double* vk, double* scal, int* ikmax,
+                                   double* vgrid) {
+  RefSim* s = (RefSim*)h;
+  const int np = s->cfg.npart;
+  OptEwaldSum e(*s->simInfo->getSuperCell(), np, rcut, kcut, 4 * kcut, 8);
+  for (int i = 0; i < np; ++i) e.getQArray()(i) = s->simInfo->getPartSpecies(i).charge;
+  e.evalSelfEnergy();
+  *totk = e.totk;
+  if (kvec)
+    for (int i = 0; i < e.totk; ++i) {
+      kvec[3 * i] = e.kvec(i)[0];
+      kvec[3 * i + 1] = e.kvec(i)[1];
+      kvec[3 * i + 2] = e.kvec(i)[2];
+      vk[i] = e.vk(i);
+    }
+  scal[0] = e.oneOver2V;
+  scal[1] = e.selfEnergy;
+  for (int d = 0; d < 3; ++d) ikmax[d] = e.ikmax[d];
+  if (vgrid) {
+    const double dr = rcut / 1000;
+    vgrid[0] = -e.evalFR0() / epsilon;
+    for (int i = 1; i < 1001; ++i) vgrid[i] = -e.evalFR(i * dr) / epsilon;
+  }
   return 0;
 }
 

@@ -129,6 +129,7 @@ struct pimc_engine {
   cudaGraphExec_t graph = nullptr;
   int graph_attempts = -1, graph_steps = -1;
   Layout lay{};
+  Layout est_lay{};  // estimator kernels
   LayoutOpts lay_opts{};
   int ctas_cap = 0;
   int minb = 2;  // register-budget variant of the section kernel
@@ -374,6 +375,41 @@ void set_smem_caps() {
                        200 * 1024);
 }
 
+// Shared memory of the estimator kernels: one staged slice (in the section
+// arrays' places), the reduction buffer, charges and the e^{ik.r} tables of the
+// largest k-list among the systems' and an estimator's own (ikmax_extra).
+Layout estimator_layout(const std::vector<DevSys>& sys, const int* ikmax_extra) {
+  int nsec = 1, np = 1, ik[3] = {0, 0, 0};
+  for (const DevSys& d : sys) {
+    nsec = std::max(nsec, d.nsec);
+    np = std::max(np, d.npart);
+    if (d.ewald)
+      for (int a = 0; a < 3; ++a) ik[a] = std::max(ik[a], d.ikmax[a]);
+  }
+  if (ikmax_extra)
+    for (int a = 0; a < 3; ++a) ik[a] = std::max(ik[a], ikmax_extra[a]);
+  Layout L{};
+  int off = 0;
+  auto take = [&](int n) {
+    const int o = off;
+    off += (n + 1) & ~1;
+    return o;
+  };
+  L.s1 = take(3 * nsec * np);
+  L.s2 = L.s1;
+  L.mv = take(3 * nsec);
+  L.red = take(64);
+  L.q = take(np);
+  L.ewt = take(2 * ((ik[0] + 1) + (2 * ik[1] + 1) + (2 * ik[2] + 1)) * (np + 1));
+  L.ictl = take(C_NCTL + 2);
+  L.dm = L.ndm = L.edet = L.dist = L.ndist = L.red;
+  L.ecache = L.ncol = -1;
+  L.nodescr = 0;
+  L.nodescr_in_smem = 1;
+  L.total = off;
+  return L;
+}
+
 int device_check(int& nsm) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(PIMC_ERR_NO_DEVICE, "no CUDA device");
@@ -497,6 +533,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
     delete e;
     return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
   }
+  e->est_lay = estimator_layout(e->hsys, nullptr);
   // device buffers
   if (e->d_ugrid.alloc(pool.size()) || e->d_ugrid32.alloc(pool.size())) {
     delete e;
@@ -681,8 +718,8 @@ int enqueue_thermo(pimc_engine* e, cudaStream_t st, int row) {
   P.partial = e->d_partial.p;
   P.nchunk = kThermoChunks;
   P.nrep = e->nrep;
-  P.lay = e->lay;
-  thermo_kernel<<<dim3(kThermoChunks, e->nrep), kBlock, e->lay.total * 8, st>>>(P);
+  P.lay = e->est_lay;
+  thermo_kernel<<<dim3(kThermoChunks, e->nrep), kBlock, e->est_lay.total * 8, st>>>(P);
   thermo_reduce_kernel<<<(e->nrep + 127) / 128, 128, 0, st>>>(
       e->d_sys.p, nullptr, e->d_partial.p, kThermoChunks, e->nrep,
       e->d_energy.p + (size_t)row * e->nrep);
@@ -764,6 +801,86 @@ int pimc_thermo_energy(pimc_engine* e, double* host_energy) {
                      cudaMemcpyDeviceToHost, e->stream));
   CU(cudaStreamSynchronize(e->stream));
   return PIMC_OK;
+}
+
+namespace {
+// Runs one estimator kernel over every replica (64 chunks each), reduces the
+// partials per replica (÷ M) and copies the energies to the host.
+enum { kEstVirial = 0, kEstCoulomb = 1 };
+int run_estimator(pimc_engine* e, int which, EstimatorParams P, const Layout& L, double* host) {
+  if (e->d_partial.n < (size_t)e->nrep * kThermoChunks &&
+      e->d_partial.alloc((size_t)e->nrep * kThermoChunks))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc energy partials");
+  double* d_out = nullptr;
+  CU(cudaMallocAsync(&d_out, e->nrep * sizeof(double), e->stream));
+  P.sys = e->d_sys.p;
+  P.paths = e->d_paths.p;
+  P.partial = e->d_partial.p;
+  P.nchunk = kThermoChunks;
+  P.nrep = e->nrep;
+  P.lay = L;
+  const dim3 grid(kThermoChunks, e->nrep);
+  if (which == kEstVirial) {
+    cudaFuncSetAttribute(virial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    virial_kernel<<<grid, kBlock, L.total * 8, e->stream>>>(P);
+  } else {
+    cudaFuncSetAttribute(coulomb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    coulomb_kernel<<<grid, kBlock, L.total * 8, e->stream>>>(P);
+  }
+  thermo_reduce_kernel<<<(e->nrep + 127) / 128, 128, 0, e->stream>>>(
+      e->d_sys.p, nullptr, e->d_partial.p, kThermoChunks, e->nrep, d_out);
+  e->launches += 2;
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(host, d_out, e->nrep * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaFreeAsync(d_out, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return PIMC_OK;
+}
+}  // namespace
+
+int pimc_virial_energy(pimc_engine* e, int nwindow, double* host_energy) {
+  if (!e || e->server || nwindow < 1 || !host_energy) return fail(PIMC_ERR_INVALID, "bad argument");
+  EstimatorParams P{};
+  P.nwindow = nwindow;
+  return run_estimator(e, kEstVirial, P, e->est_lay, host_energy);
+}
+
+int pimc_coulomb_energy(pimc_engine* e, double epsilon, double* host_energy) {
+  if (!e || e->server || !(epsilon > 0) || !host_energy)
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  EstimatorParams P{};
+  P.epsilon = epsilon;
+  return run_estimator(e, kEstCoulomb, P, e->est_lay, host_energy);
+}
+
+int pimc_ewald_coulomb_energy(pimc_engine* e, double epsilon, double rcut,
+                              const pimc_ewald_table* est, const double* vgrid,
+                              double* host_energy) {
+  if (!e || e->server || !(epsilon > 0) || !(rcut > 0) || !est || !vgrid || !host_energy ||
+      est->totk < 0 || (est->totk > 0 && (!est->kvec || !est->vk)))
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  DevBuf<int> kv;
+  DevBuf<double> vk, vg;
+  if (kv.alloc(3 * std::max(est->totk, 1)) || vk.alloc(std::max(est->totk, 1)) || vg.alloc(1001))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc estimator tables");
+  if (est->totk > 0) {
+    CU(cudaMemcpy(kv.p, est->kvec, 3 * est->totk * sizeof(int), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(vk.p, est->vk, est->totk * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CU(cudaMemcpy(vg.p, vgrid, 1001 * sizeof(double), cudaMemcpyHostToDevice));
+  EstimatorParams P{};
+  P.epsilon = epsilon;
+  P.vgrid = vg.p;
+  P.rcut = rcut;
+  P.totk = est->totk;
+  P.kvec = kv.p;
+  P.vk = vk.p;
+  P.one_over_2v = est->one_over_2v;
+  P.self_energy = est->self_energy;
+  for (int a = 0; a < 3; ++a) P.ikmax[a] = est->ikmax[a];
+  const Layout L = estimator_layout(e->hsys, est->ikmax);
+  const int rc = run_estimator(e, kEstCoulomb, P, L, host_energy);
+  return rc;
 }
 
 int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy) {

@@ -183,6 +183,265 @@ __device__ __forceinline__ void round_robin_pair(int n, int rd, int k, int& a, i
   }
 }
 
+// ------------------------------------------------------ virial estimator
+// The forces fm, fp of getBeadAction summed over the actions, for the link
+// ending at slice t of particle ip: SpringAction (src/action/SpringAction.cc:112-123),
+// SHOAction (src/action/SHOAction.cc:71-105), PrimSHOAction
+// (src/action/PrimSHOAction.cc:65-81), PairAction (src/action/PairAction.cc:509-599,
+// uk0CalcDerivatives :641-660).  The Ewald term and FixedNodeAction add none.
+static __device__ void bead_forces(const DevSys& s, const double* path, int ip, int t, double* fm,
+                                   double* fp) {
+  const int np = s.npart, M = s.nslice;
+  const int tm = t == 0 ? M - 1 : t - 1, tp = t == M - 1 ? 0 : t + 1;
+  const double* b1 = path + ((size_t)t * np + ip) * 3;
+  const double* b0 = path + ((size_t)tm * np + ip) * 3;
+  const double* b2 = path + ((size_t)tp * np + ip) * 3;
+  const int sp = species_of(s, ip);
+  const double tau = s.tau;
+  for (int d = 0; d < 3; ++d) fm[d] = fp[d] = 0.0;
+  double dmx = b1[0] - b0[0], dmy = b1[1] - b0[1], dmz = b1[2] - b0[2];
+  pbc(s, dmx, dmy, dmz);
+  double dpx = b1[0] - b2[0], dpy = b1[1] - b2[1], dpz = b1[2] - b2[2];
+  pbc(s, dpx, dpy, dpz);
+  const double dm[3] = {dmx, dmy, dmz}, dp[3] = {dpx, dpy, dpz};
+  if (s.spring)
+    for (int d = 0; d < 3; ++d) {
+      fm[d] -= dm[d] / (2 * s.lambda[sp] * tau);
+      fp[d] -= dp[d] / (2 * s.lambda[sp] * tau);
+    }
+  const double om = s.sho_omega[sp];
+  if (om > 0) {
+    const double m = s.mass[sp], cschwt = s.sho_csch[sp], coshwt = s.sho_cosh0[sp];
+    const double tin = 1.0 / tau;
+    for (int d = 0; d < 3; ++d) {
+      fm[d] -= m * om * (b1[d] * coshwt - b0[d]) * cschwt - m * dm[d] * tin;
+      fp[d] -= m * om * (b1[d] * coshwt - b2[d]) * cschwt - m * dp[d] * tin;
+    }
+  }
+  if (s.prim_a[sp] != 0 || s.prim_b[sp] != 0) {
+    const double x2 = b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2];
+    const double c = -0.5 * (2 * s.prim_a[sp] + 4 * s.prim_b[sp] * x2) * tau;
+    for (int d = 0; d < 3; ++d) {
+      fm[d] += c * b1[d];
+      fp[d] += c * b1[d];
+    }
+  }
+  if (!s.coulomb) return;
+  for (int ti = 0; ti < s.ntab; ++ti) {
+    const DevTable& tb = s.tab[ti];
+    int jb, je;
+    if (ip >= tb.ifirst1 && ip < tb.ifirst1 + tb.npart1) {
+      jb = tb.ifirst2;
+      je = tb.ifirst2 + tb.npart2;
+    } else if (ip >= tb.ifirst2 && ip < tb.ifirst2 + tb.npart2) {
+      jb = tb.ifirst1;
+      je = tb.ifirst1 + tb.npart1;
+    } else {
+      continue;
+    }
+    for (int j = jb; j < je; ++j) {
+      if (j == ip) continue;
+      const double* c1 = path + ((size_t)t * np + j) * 3;
+      double delta[3] = {b1[0] - c1[0], b1[1] - c1[1], b1[2] - c1[2]};
+      pbc(s, delta[0], delta[1], delta[2]);
+      const double r = sqrt(dot3(delta[0], delta[1], delta[2], delta[0], delta[1], delta[2]));
+      for (int side = 0; side < 2; ++side) {
+        const double* bo = side == 0 ? b0 : b2;
+        const double* co = path + ((size_t)(side == 0 ? tm : tp) * np + j) * 3;
+        double o[3] = {bo[0] - co[0], bo[1] - co[1], bo[2] - co[2]};
+        pbc(s, o[0], o[1], o[2]);
+        const double ro = sqrt(dot3(o[0], o[1], o[2], o[0], o[1], o[2]));
+        const double q = 0.5 * (r + ro);
+        const double sv[3] = {delta[0] - o[0], delta[1] - o[1], delta[2] - o[2]};
+        const double s2 = dot3(sv[0], sv[1], sv[2], sv[0], sv[1], sv[2]) / (q * q);
+        // uk0CalcDerivatives: the q and s^2 derivatives of the off-diagonal series
+        int i;
+        double x;
+        tab_locate(tb, q, i, x);
+        const double* g0 = tb.ugrid + (size_t)i * 2 * tb.ndata;
+        const double* g1 = g0 + 2 * tb.ndata;
+        double uq = 0, us2 = 0;
+        for (int k = tb.norder; k >= 0; k--) uq = uq * s2 + (__ldg(g1 + k) - __ldg(g0 + k));
+        uq *= tb.logrratioinv * tb.rgridinv / (q * tb.rgridinv);
+        for (int k = tb.norder; k > 0; k--)
+          us2 = us2 * s2 + k * ((1 - x) * __ldg(g0 + k) + x * __ldg(g1 + k));
+        double* f = side == 0 ? fm : fp;
+        for (int d = 0; d < 3; ++d)
+          f[d] -= uq * delta[d] / (2 * r) + us2 * (2 * sv[d] / (q * q) - s2 * delta[d] / (q * r));
+      }
+    }
+  }
+}
+
+struct EstimatorParams {
+  const DevSys* sys;
+  const double* paths;
+  double* partial;  // [nrep][nchunk]
+  int nchunk;
+  int nrep;
+  Layout lay;
+  int nwindow;  // virial
+  // Coulomb estimators: epsilon; with vgrid, the optimized-Ewald form (short
+  // range tabulated to rcut, long range from this k-list)
+  double epsilon;
+  const double* vgrid;
+  double rcut;
+  int totk;
+  const int* kvec;
+  const double* vk;
+  double one_over_2v, self_energy;
+  int ikmax[3];
+};
+
+// VirialEnergyEstimator::handleLink / endCalc (src/estimator/VirialEnergyEstimator.cc:34-79).
+// One CTA per (chunk of windows, replica); one thread per (window, particle)
+// runs the window's links in order, so each window's running sums are pi-qmc's.
+__global__ void __launch_bounds__(kBlock) virial_kernel(EstimatorParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  {
+    const int* src = (const int*)(P.sys + blockIdx.y);
+    int* dst = (int*)&S;
+    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) S.mixed = 0;  // the estimator is evaluated in FP64
+  __syncthreads();
+  const DevSys& s = S;
+  const double* path = P.paths + s.path_offset;
+  const int M = s.nslice, np = s.npart, nw = P.nwindow;
+  const int nwin = (M + nw - 1) / nw;
+  const int per = (nwin + P.nchunk - 1) / P.nchunk;
+  const int w0 = blockIdx.x * per, w1 = min(nwin, w0 + per);
+  Smem m = carve(smem, P.lay, s, nullptr);
+  const double tau = s.tau, h = 1 / (2 * tau);
+  double part = 0.0;
+  for (int it = threadIdx.x; it < (w1 - w0) * np; it += blockDim.x) {
+    const int w = w0 + it / np, ip = it % np;
+    double r0[3] = {0, 0, 0}, rav[3] = {0, 0, 0}, fav[3] = {0, 0, 0};
+    double e = 0.0;
+    for (int t = w * nw; t < min(M, (w + 1) * nw); ++t) {
+      const int k = t - w * nw;
+      const int thisWindow = (t / nw < (M - 1) / nw) ? nw : (M - 1) % nw + 1;
+      const int tm = t == 0 ? M - 1 : t - 1;
+      const double* b1 = path + ((size_t)t * np + ip) * 3;
+      const double* b0 = path + ((size_t)tm * np + ip) * 3;
+      double r[3] = {b1[0] - b0[0], b1[1] - b0[1], b1[2] - b0[2]};
+      pbc(s, r[0], r[1], r[2]);
+      double fm[3], fp[3];
+      bead_forces(s, path, ip, t, fm, fp);
+      double f[3];
+      for (int d = 0; d < 3; ++d) {
+        rav[d] += r[d];
+        r0[d] += (thisWindow - k) * r[d] / thisWindow;
+        f[d] = fm[d] + fp[d];
+        fav[d] += f[d];
+      }
+      e += link_utau(s, path, ip, t);
+      e += -(1. - 1. / thisWindow) * (3 / (2 * tau)) - h * dot3(f[0], f[1], f[2], rav[0], rav[1], rav[2]);
+    }
+    e += h * dot3(fav[0], fav[1], fav[2], r0[0], r0[1], r0[2]);
+    part += e;
+  }
+  double tot = block_sum(part, m.red);
+  if (s.coulomb && s.ewald) {  // CoulombAction adds the long-range utau at ipart == 0
+    for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
+    for (int t = w0 * nw; t < min(M, w1 * nw); ++t) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        const double* b = path + ((size_t)t * np + i) * 3;
+        m.s1x[i] = b[0];
+        m.s1y[i] = b[1];
+        m.s1z[i] = b[2];
+      }
+      __syncthreads();
+      tot += ewald_slice_energy(s, m, 0) / s.epsilon;
+    }
+  }
+  if (threadIdx.x == 0) P.partial[(size_t)blockIdx.y * P.nchunk + blockIdx.x] = tot;
+}
+
+// CoulombEnergyEstimator::handleLink (src/estimator/CoulombEnergyEstimator.cc:30-40) and,
+// with a vgrid, EwaldCoulombEstimator::handleLink's optimized-Ewald branch
+// (src/estimator/EwaldCoulombEstimator.cc:102-140): every pair once per slice,
+// q_i q_j / (eps r) (the short-range form adds the tabulated -f(r)/eps with
+// pi-qmc's interpolation weight x = r - i dr, and stops at rcut), plus each
+// slice's long-range sum for the Ewald form.
+__global__ void __launch_bounds__(kBlock) coulomb_kernel(EstimatorParams P) {
+  extern __shared__ double smem[];
+  __shared__ DevSys S;
+  {
+    const int* src = (const int*)(P.sys + blockIdx.y);
+    int* dst = (int*)&S;
+    for (int i = threadIdx.x; i < (int)(sizeof(DevSys) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  const bool ew = P.vgrid != nullptr;
+  if (threadIdx.x == 0 && ew) {  // the estimator's own Ewald sum
+    S.totk = P.totk;
+    S.kvec = P.kvec;
+    S.vk = P.vk;
+    S.one_over_2v = P.one_over_2v;
+    S.self_energy = P.self_energy;
+    for (int d = 0; d < 3; ++d) {
+      S.ikmax[d] = P.ikmax[d];
+      S.deltak[d] = 2 * 3.14159265358979 * S.cellb[d];
+    }
+  }
+  __syncthreads();
+  const DevSys& s = S;
+  const double* path = P.paths + s.path_offset;
+  const int M = s.nslice, np = s.npart;
+  const int per = (M + P.nchunk - 1) / P.nchunk;
+  const int t0 = blockIdx.x * per, t1 = min(M, t0 + per);
+  Smem m = carve(smem, P.lay, s, nullptr);
+  const double eps = P.epsilon, dr = P.rcut / 1000, drinv = 1. / dr;
+  double part = 0.0;
+  if (np > 1) {
+    const int ne = np + (np & 1), per_round = ne / 2, nrd = ne - 1;
+    const int items = (t1 - t0) * nrd * per_round;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int t = t0 + it / (nrd * per_round);
+      const int rest = it % (nrd * per_round);
+      int a, b;
+      round_robin_pair(ne, rest / per_round, rest % per_round, a, b);
+      if (a >= np || b >= np) continue;
+      const int i = max(a, b), j = min(a, b);  // pi-qmc's delta = r_i - r_j, j < i
+      const double* bi = path + ((size_t)t * np + i) * 3;
+      const double* bj = path + ((size_t)t * np + j) * 3;
+      double dx = bi[0] - bj[0], dy = bi[1] - bj[1], dz = bi[2] - bj[2];
+      pbc(s, dx, dy, dz);
+      const double r = sqrt(dot3(dx, dy, dz, dx, dy, dz));
+      const double qq = s.charge[species_of(s, i)] * s.charge[species_of(s, j)];
+      if (!ew) {
+        part += qq / (eps * r);
+      } else if (r < P.rcut) {
+        const int ig = (int)(r * drinv);
+        const double x = r - ig * dr;
+        part += qq * (1. / (r * eps) + (1 - x) * P.vgrid[ig] + x * P.vgrid[ig + 1]);
+      }
+    }
+  }
+  double tot = block_sum(part, m.red);
+  if (ew) {
+    for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
+    for (int t = t0; t < t1; ++t) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        const double* b = path + ((size_t)t * np + i) * 3;
+        m.s1x[i] = b[0];
+        m.s1y[i] = b[1];
+        m.s1z[i] = b[2];
+      }
+      __syncthreads();
+      tot += ewald_slice_energy(s, m, 0) / eps;
+    }
+  }
+  if (threadIdx.x == 0) P.partial[(size_t)blockIdx.y * P.nchunk + blockIdx.x] = tot;
+}
+
 // Per-replica energy from the chunk partials: chunks summed in order, then
 // divided by the slice count (ThermoEnergyEstimator's normalisation).
 __global__ void thermo_reduce_kernel(const DevSys* sys, const int* index, const double* partial,

@@ -396,6 +396,34 @@ int pimc_coulomb_tables(const pimc_system* sys, int norder, int ngpts, double rm
   return PIMC_OK;
 }
 
+// The optimized Ewald sum an EwaldCoulombEstimator builds for itself
+// (src/estimator/EwaldCoulombEstimator.cc:60-90, the same fit as the action's with
+// the estimator's rcut and kcut): its k-list table and the 1001-point grid
+// vgrid[i] = -f(i rcut/1000)/epsilon (vgrid[0] = -f(0)/epsilon).  The table stays
+// valid until the next call on the same thread.
+int pimc_ewald_estimator_tables(const pimc_system* sys, double rcut, double kcut, double epsilon,
+                                const pimc_ewald_table** est, double* vgrid) {
+  if (!sys || !est || !vgrid || !(rcut > 0) || !(kcut > 0) || !(epsilon > 0))
+    return PIMC_ERR_INVALID;
+  static thread_local OptEwald E;
+  static thread_local pimc_ewald_table et;
+  std::vector<double> q;
+  for (int s = 0; s < sys->nspecies; ++s)
+    for (int k = 0; k < sys->spec_count[s]; ++k) q.push_back(sys->spec_charge[s]);
+  if (!build_opt_ewald(sys->cell, q.data(), sys->npart, rcut, kcut, E)) return PIMC_ERR_INVALID;
+  const double dr = rcut / 1000;
+  vgrid[0] = -E.coef[0] / epsilon;
+  for (int i = 1; i < 1001; ++i) vgrid[i] = -E.evalFR(i * dr) / epsilon;
+  et.totk = (int)E.vk.size();
+  et.kvec = E.kvec.data();
+  et.vk = E.vk.data();
+  et.one_over_2v = E.oneOver2V;
+  et.self_energy = E.selfEnergy;
+  for (int a = 0; a < 3; ++a) et.ikmax[a] = E.ikmax[a];
+  *est = &et;
+  return PIMC_OK;
+}
+
 // The short-range polynomial coefficients of the last Ewald table built.
 int pimc_ewald_coefficients(double* coef, int n) {
   if (!g_tables.has_ewald) return PIMC_ERR_INVALID;

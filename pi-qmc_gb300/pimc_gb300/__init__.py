@@ -132,6 +132,13 @@ def lib():
                                           C.POINTER(C.c_uint32)]
         L.pimc_thermo_energy.argtypes = [P, D]
         L.pimc_run_steps.argtypes = [P, I, I, D]
+        L.pimc_virial_energy.argtypes = [P, I, D]
+        L.pimc_coulomb_energy.argtypes = [P, C.c_double, D]
+        L.pimc_ewald_coulomb_energy.argtypes = [P, C.c_double, C.c_double,
+                                                C.POINTER(EwaldTable), D, D]
+        L.pimc_ewald_estimator_tables.argtypes = [C.POINTER(System), C.c_double, C.c_double,
+                                                  C.c_double, C.POINTER(C.POINTER(EwaldTable)),
+                                                  D]
         L.pimc_action_difference.argtypes = [P, I, I, D, D, C.POINTER(C.c_int), D]
         L.pimc_node_evaluate.argtypes = [P, I, I, D, D, D, D, D, C.POINTER(C.c_int)]
         L.pimc_node_scale.argtypes = [P, I, I, D]
@@ -375,6 +382,26 @@ class Engine:
         _check(lib().pimc_thermo_energy(self.h, _dp(out)))
         return out
 
+    def virial_energy(self, nwindow=1):
+        out = np.zeros(self.nreplica)
+        _check(lib().pimc_virial_energy(self.h, nwindow, _dp(out)))
+        return out
+
+    def coulomb_energy(self, epsilon=1.0):
+        out = np.zeros(self.nreplica)
+        _check(lib().pimc_coulomb_energy(self.h, epsilon, _dp(out)))
+        return out
+
+    def ewald_coulomb_energy(self, epsilon, rcut, est_ewald, vgrid):
+        """The optimized-Ewald Coulomb estimator with its own table (dict as
+        returned by ewald_estimator_tables) and 1001-point grid."""
+        ew, keep = ewald_struct(est_ewald)
+        vg = np.ascontiguousarray(vgrid, np.float64)
+        out = np.zeros(self.nreplica)
+        _check(lib().pimc_ewald_coulomb_energy(self.h, epsilon, rcut, C.byref(ew), _dp(vg),
+                                               _dp(out)))
+        return out
+
     # Action / NodeModel level ---------------------------------------------
     def action_difference(self, level, sections, movings, iparts):
         sections = np.ascontiguousarray(sections, np.float64)
@@ -524,3 +551,19 @@ def coulomb_tables(system_kw, norder=3, ngpts=0, rmin=0.0, rmax=0.0, ewald_rcut=
                      vk=np.ctypeslib.as_array(e.vk, shape=(e.totk,)).copy(),
                      one_over_2v=e.one_over_2v, self_energy=e.self_energy, ikmax=list(e.ikmax))
     return tables, ewald
+
+
+def ewald_estimator_tables(system_kw, rcut, kcut, epsilon=1.0):
+    """The optimized Ewald sum an EwaldCoulombEstimator builds for itself: its
+    k-list table (dict) and the 1001-point grid -f(i rcut/1000)/epsilon."""
+    L = lib()
+    s = system_from_kw(system_kw)
+    ep = C.POINTER(EwaldTable)()
+    vg = np.zeros(1001)
+    _check(L.pimc_ewald_estimator_tables(C.byref(s), rcut, kcut, epsilon, C.byref(ep), _dp(vg)))
+    e = ep.contents
+    ew = dict(totk=e.totk,
+              kvec=np.ctypeslib.as_array(e.kvec, shape=(e.totk * 3,)).reshape(-1, 3).copy(),
+              vk=np.ctypeslib.as_array(e.vk, shape=(e.totk,)).copy(),
+              one_over_2v=e.one_over_2v, self_energy=e.self_energy, ikmax=list(e.ikmax))
+    return ew, vg

@@ -6,7 +6,9 @@ the configuration, the initial path, the pair-action and Ewald tables the
 reference built, per-attempt records (section start, moving particle, rejecting
 level, per-level action differences and mover log transition ratios), the
 final path (stored as its difference from the initial path, which compresses)
-and the thermodynamic energy estimator of the final path.
+and, on the final path, the thermodynamic, virial (windows 1, 4, 16) and
+Coulomb energy estimators (direct, and for periodic cases the optimized-Ewald
+estimator together with the Ewald table and short-range grid it built).
 
 The fixtures let machines without the reference tree (the GPU machine) pin the C++
 restatement and the CUDA engine against the reference's own outputs.
@@ -25,6 +27,9 @@ sys.path.insert(0, os.path.join(REPO, "tests"))
 
 import oracle_lib as O  # noqa: E402
 import workloads as W  # noqa: E402
+
+
+VIRIAL_WINDOWS = (1, 4, 16)
 
 
 def run_case(name, kw, init, nattempt):
@@ -58,6 +63,20 @@ def run_case(name, kw, init, nattempt):
     for k in ("ifirst1", "ifirst2", "ipart", "reject_level", "ds", "ds_node", "lnt"):
         out["rec_" + k] = recs[k]
     out["naccepted"] = recs["naccepted"]
+    out["est_virial_windows"] = np.array(VIRIAL_WINDOWS, np.int32)
+    out["est_virial"] = np.array([ref.virial_energy(w) for w in VIRIAL_WINDOWS])
+    out["est_coulomb"] = np.array(ref.coulomb_energy(1.0))
+    if kw.get("ewald"):
+        lbox = kw["cell"] if not isinstance(kw["cell"], (list, tuple)) else kw["cell"][0]
+        rcut, kcut = lbox / 2, 5 * 2 * np.pi / lbox
+        est, vg = ref.estimator_ewald(1.0, rcut, kcut)
+        out["estew_params"] = np.array([1.0, rcut, kcut])
+        out["estew_kvec"] = est["kvec"]
+        out["estew_vk"] = est["vk"]
+        out["estew_scalars"] = np.array([est["one_over_2v"], est["self_energy"]])
+        out["estew_ikmax"] = np.array(est["ikmax"], np.int32)
+        out["estew_vgrid"] = vg
+        out["est_ewald_coulomb"] = np.array(ref.ewald_coulomb_energy(1.0, rcut, kcut))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print(f"{name}: {nattempt} attempts, {recs['naccepted']} accepted, "

@@ -25,7 +25,21 @@ def load(name):
                   ikmax=[int(v) for v in z["ewald_ikmax"]], coef=z["ewald_coef"])
     rec = {k: z["rec_" + k] for k in ("ifirst1", "ifirst2", "ipart", "reject_level", "ds",
                                       "ds_node", "lnt")}
-    return dict(kw=kw, tables=tabs, ewald=ew, path0=z["path0"],
+    est = {}
+    if "est_virial" in z:
+        est["virial"] = dict(zip((int(w) for w in z["est_virial_windows"]),
+                                 (float(v) for v in z["est_virial"])))
+        est["coulomb"] = float(z["est_coulomb"])
+    if "estew_kvec" in z:
+        prm = z["estew_params"]
+        est["ewald"] = dict(epsilon=float(prm[0]), rcut=float(prm[1]), kcut=float(prm[2]),
+                            table=dict(totk=len(z["estew_vk"]), kvec=z["estew_kvec"],
+                                       vk=z["estew_vk"],
+                                       one_over_2v=float(z["estew_scalars"][0]),
+                                       self_energy=float(z["estew_scalars"][1]),
+                                       ikmax=[int(v) for v in z["estew_ikmax"]]),
+                            vgrid=z["estew_vgrid"], energy=float(z["est_ewald_coulomb"]))
+    return dict(kw=kw, tables=tabs, ewald=ew, path0=z["path0"], estimators=est,
                 path1=z["path0"] + z["dpath"], energy0=float(z["energy0"]),
                 energy1=float(z["energy1"]), records=rec, nattempt=int(z["nattempt"]),
                 naccepted=int(z["naccepted"]))

@@ -288,3 +288,22 @@ def test_register_variants_bit_identical(pimc):
     for o in out[1:]:
         for x, y in zip(out[0], o):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("case", ["dot2_full", "dot4_fn", "heg8", "heg54", "dot20_fn"])
+def test_estimators_match_golden(pimc, case):
+    # Virial, Coulomb and optimized-Ewald Coulomb estimators through the ABI on
+    # the final golden path against pi-qmc's own estimator values (the engine
+    # sums pairs and windows in parallel: 1e-11 relative).
+    g = golden_io.load(case)
+    est = g["estimators"]
+    e = engine_for(pimc, g, nreplica=2)
+    e.upload_paths([g["path1"], g["path1"]])
+    for w, v in est["virial"].items():
+        got = e.virial_energy(w)
+        assert np.allclose(got, v, rtol=1e-11, atol=1e-11), (w, got, v)
+    assert np.allclose(e.coulomb_energy(1.0), est["coulomb"], rtol=1e-12)
+    if "ewald" in est:
+        x = est["ewald"]
+        got = e.ewald_coulomb_energy(x["epsilon"], x["rcut"], x["table"], x["vgrid"])
+        assert np.allclose(got, x["energy"], rtol=1e-11), (got, x["energy"])

@@ -144,3 +144,41 @@ def test_port_matches_reference_action_levels():
             a = ref.action_diff(level, sec, mov, ip)
             b = port.action_diff(level, sec, mov, ip)
             assert abs(a - b) <= 1e-12 * max(abs(a), 1.0)
+
+
+@pytest.mark.parametrize("case", list(W.GOLDEN_CASES))
+def test_port_estimators_match_golden(case):
+    # Virial (windows 1, 4, 16), direct Coulomb and optimized-Ewald Coulomb
+    # estimators of the restatement on the final golden path against the values
+    # pi-qmc's own estimator classes produced.
+    g = golden_io.load(case)
+    est = g["estimators"]
+    port = O.PortOracle(O.make_config(**g["kw"]), g["tables"], g["ewald"])
+    port.set_path(g["path1"])
+    for w, v in est["virial"].items():
+        assert port.virial_energy(w) == pytest.approx(v, rel=1e-12, abs=1e-12), w
+    assert est["virial"][1] == pytest.approx(g["energy1"], rel=1e-12)  # window 1 = thermo
+    assert port.coulomb_energy(1.0) == pytest.approx(est["coulomb"], rel=1e-13)
+    if "ewald" in est:
+        e = est["ewald"]
+        got = port.ewald_coulomb_energy(e["epsilon"], e["rcut"], e["table"], e["vgrid"])
+        assert got == pytest.approx(e["energy"], rel=1e-12)
+
+
+def test_estimator_ewald_builder_against_reference():
+    # The engine's own optimized-Ewald fit for the estimator: same k-list as
+    # pi-qmc's, coefficients set by a differently conditioned solve, so the
+    # tables agree to ~1e-3 and the energy to ~2e-4 (pi-qmc's coefficients are
+    # themselves rounding-determined for this system).
+    import pimc_gb300
+    g = golden_io.load("heg8")
+    e = g["estimators"]["ewald"]
+    ew, vg = pimc_gb300.ewald_estimator_tables(g["kw"], e["rcut"], e["kcut"], e["epsilon"])
+    assert ew["totk"] == e["table"]["totk"]
+    assert np.array_equal(ew["kvec"], e["table"]["kvec"])
+    assert np.max(np.abs(ew["vk"] - e["table"]["vk"])) <= 5e-3 * np.abs(e["table"]["vk"]).max()
+    assert np.max(np.abs(vg - e["vgrid"])) <= 5e-3 * np.abs(e["vgrid"]).max()
+    port = O.PortOracle(O.make_config(**g["kw"]), g["tables"], g["ewald"])
+    port.set_path(g["path1"])
+    got = port.ewald_coulomb_energy(e["epsilon"], e["rcut"], ew, vg)
+    assert got == pytest.approx(e["energy"], rel=1e-3)
