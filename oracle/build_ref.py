@@ -38,7 +38,8 @@ SOURCES = [
     "advancer/PermutationChooser.cc", "stats/AccRejEstimator.cc",
     "estimator/VirialEnergyEstimator.cc", "estimator/CoulombEnergyEstimator.cc",
     "estimator/EwaldCoulombEstimator.cc", "stats/ScalarEstimator.cc",
-    "stats/SimpleScalarAccumulator.cpp",
+    "stats/SimpleScalarAccumulator.cpp", "advancer/DisplaceMoveSampler.cc",
+    "advancer/DoubleDisplaceMoveSampler.cc", "advancer/UniformMover.cc",
 ]
 
 FLAGS = ["-std=gnu++98", "-O2", "-fPIC", "-w", "-ffp-contract=off", "-DHAVE_CONFIG_H"]

@@ -59,6 +59,16 @@ typedef struct {
   double lnt[ORA_MAX_LEVEL + 1];     /* mover ln(T_old/T_new) per level */
 } ora_record;
 
+/* One attempted rigid displacement of whole particle paths. */
+#define ORA_MAX_MOVING 4
+typedef struct {
+  int ipart[ORA_MAX_MOVING];       /* moving particles (nmoving used) */
+  double disp[ORA_MAX_MOVING][3];  /* their displacements */
+  double ds;                       /* Action difference (both halves for the double form) */
+  double ds_node;                  /* DoubleAction difference */
+  int accepted;
+} ora_drecord;
+
 /* Pair-action table handed to the port (the reference builds its own). */
 typedef struct {
   int ngpts, norder;

@@ -44,6 +44,25 @@ class OraRecord(C.Structure):
     ]
 
 
+MAXMOV = 4
+
+
+class OraDRecord(C.Structure):
+    _fields_ = [("ipart", C.c_int * MAXMOV), ("disp", (C.c_double * 3) * MAXMOV),
+                ("ds", C.c_double), ("ds_node", C.c_double), ("accepted", C.c_int)]
+
+
+def drecords_to_numpy(recs, n, nmoving):
+    return {
+        "ipart": np.array([[recs[i].ipart[k] for k in range(nmoving)] for i in range(n)],
+                          np.int32),
+        "disp": np.array([[list(recs[i].disp[k]) for k in range(nmoving)] for i in range(n)]),
+        "ds": np.array([recs[i].ds for i in range(n)]),
+        "ds_node": np.array([recs[i].ds_node for i in range(n)]),
+        "accepted": np.array([recs[i].accepted for i in range(n)], np.int32),
+    }
+
+
 class OraPairTable(C.Structure):
     _fields_ = [("ngpts", C.c_int), ("norder", C.c_int), ("rgridinv", C.c_double),
                 ("logrratioinv", C.c_double), ("ugrid", C.POINTER(C.c_double))]
@@ -156,6 +175,15 @@ class _Base:
         r["naccepted"] = nacc
         return r
 
+    def run_displace(self, n, dist, nmoving=1, species=-1, first_attempt=0):
+        """n rigid-displacement attempts (uniform box dist[3]); records per attempt."""
+        recs = (OraDRecord * max(n, 1))()
+        d = (C.c_double * 3)(*[float(x) for x in dist])
+        nacc = self._run_displace(self.h, n, first_attempt, d, nmoving, species, recs)
+        r = drecords_to_numpy(recs, n, nmoving)
+        r["naccepted"] = nacc
+        return r
+
 
 class RefOracle(_Base):
     """pi-qmc's own code (requires oracle/_ref/libpimcref.so)."""
@@ -174,6 +202,9 @@ class RefOracle(_Base):
             for f in ("ref_set_path", "ref_get_path"):
                 getattr(L, f).argtypes = [C.c_void_p, C.POINTER(C.c_double)]
             L.ref_run.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(OraRecord)]
+            L.ref_run_displace.argtypes = [C.c_void_p, C.c_int, C.c_uint32,
+                                           C.POINTER(C.c_double), C.c_int, C.c_int,
+                                           C.POINTER(OraDRecord)]
             L.ref_thermo_energy.restype = C.c_double
             L.ref_thermo_energy.argtypes = [C.c_void_p]
             L.ref_virial_energy.restype = C.c_double
@@ -221,6 +252,7 @@ class RefOracle(_Base):
         self._cfg_keep = cfg
         self.h = C.c_void_p(L.ref_create(C.byref(cfg)))
         self._get, self._set, self._run = L.ref_get_path, L.ref_set_path, L.ref_run
+        self._run_displace = L.ref_run_displace
 
     def virial_energy(self, nwindow=1):
         return self.lib().ref_virial_energy(self.h, nwindow)

@@ -89,6 +89,13 @@ extern "C" void oracle_shim_normals(double* out, int n) {
 // Unused on the bisection path; defined so the objects link.
 #include "action/interaction/PairIntegrator.h"
 #include "stats/ReportWriters.h"
+#include <cstring>
+#define protected public
+#include "advancer/DisplaceMoveSampler.h"
+#include "advancer/DoubleDisplaceMoveSampler.h"
+#undef protected
+#include "advancer/UniformMover.h"
+#include "advancer/SpeciesParticleChooser.h"
 #include "estimator/VirialEnergyEstimator.h"
 #include "estimator/CoulombEnergyEstimator.h"
 #include "estimator/EwaldCoulombEstimator.h"
@@ -104,6 +111,7 @@ void ReportWriters::reportScalarStep(ScalarEstimator*, PartitionedScalarAccumula
 
 // ---- recording wrappers ---------------------------------------------------
 static ora_record* g_rec = 0;
+static ora_drecord* g_drec = 0;
 static bool g_accepted = false;
 static int g_lowest_level = 99;
 
@@ -121,7 +129,9 @@ class RecAction : public Action {
   }
   virtual double getActionDifference(const Paths& p, const VArray& disp, int n,
                                      const IArray& idx, int f, int l) {
-    return inner->getActionDifference(p, disp, n, idx, f, l);
+    const double d = inner->getActionDifference(p, disp, n, idx, f, l);
+    if (g_drec) g_drec->ds += d;
+    return d;
   }
   virtual double getTotalAction(const Paths& p, const int level) const {
     return inner->getTotalAction(p, level);
@@ -144,6 +154,12 @@ class RecDoubleAction : public DoubleAction {
   virtual double getActionDifference(const SectionSamplerInterface& s, const int level) {
     double d = inner->getActionDifference(s, level);
     if (g_rec) g_rec->ds_node[level] = d;
+    return d;
+  }
+  virtual double getActionDifference(const Paths& p, const VArray& disp, int n,
+                                     const IArray& idx, int f, int l) {
+    const double d = inner->getActionDifference(p, disp, n, idx, f, l);
+    if (g_drec) g_drec->ds_node += d;
     return d;
   }
   virtual double getTotalAction(const Paths& p, const int level) const {
@@ -385,6 +401,44 @@ extern "C" int ref_run(void* h, int n, uint32_t first_attempt, ora_record* recs)
     r->reject_level = g_accepted ? -1 : g_lowest_level;
     if (g_accepted) ++nacc;
     g_rec = 0;
+  }
+  return nacc;
+}
+
+// Runs n rigid-displacement attempts (DisplaceMoveSampler::run with nrepeat 1,
+// src/advancer/DisplaceMoveSampler.cc:63-224; DoubleDisplaceMoveSampler for
+// fixed-node systems, src/advancer/DoubleDisplaceMoveSampler.cc:40-128) with a
+// UniformMover of box dist and a SimpleParticleChooser (species < 0) or a
+// SpeciesParticleChooser.  Returns the number accepted.
+extern "C" int ref_run_displace(void* h, int n, uint32_t first_attempt, const double* dist,
+                                int nmoving, int species, ora_drecord* recs) {
+  RefSim* s = (RefSim*)h;
+  UniformMover mover(Vec(dist[0], dist[1], dist[2]), 0);
+  ParticleChooser* pc =
+      species < 0 ? (ParticleChooser*)new SimpleParticleChooser(s->cfg.npart, nmoving)
+                  : (ParticleChooser*)new SpeciesParticleChooser(s->simInfo->getSpecies(species),
+                                                                 nmoving);
+  DisplaceMoveSampler* smp =
+      s->drec ? (DisplaceMoveSampler*)new DoubleDisplaceMoveSampler(
+                    nmoving, 1, *s->paths, *pc, mover, s->rec, s->drec, 0)
+              : new DisplaceMoveSampler(nmoving, 1, *s->paths, *pc, mover, s->rec, 0);
+  smp->getAccRejEstimator("displace");
+  int nacc = 0;
+  for (int a = 0; a < n; ++a) {
+    ora_drecord dummy;
+    ora_drecord* r = recs ? &recs[a] : &dummy;
+    memset(r, 0, sizeof(*r));
+    g_drec = r;
+    g_accepted = false;
+    shim_begin_attempt(s->cfg.seed, s->cfg.replica, first_attempt + (uint32_t)a);
+    smp->run();
+    for (int i = 0; i < nmoving && i < ORA_MAX_MOVING; ++i) {
+      r->ipart[i] = smp->movingIndex(i);
+      for (int d = 0; d < 3; ++d) r->disp[i][d] = smp->displacement(i)[d];
+    }
+    r->accepted = g_accepted ? 1 : 0;
+    if (g_accepted) ++nacc;
+    g_drec = 0;
   }
   return nacc;
 }
