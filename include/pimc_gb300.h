@@ -179,6 +179,26 @@ int pimc_replica_status(pimc_engine* e, int64_t* accepted, int64_t* attempted,
  * with the ThermoEnergyEstimator as the measurement. */
 int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy);
 
+/* ---- rigid displacement moves ------------------------------------------- */
+
+/* One attempted rigid displacement of whole particle paths. */
+typedef struct {
+  int ipart[4];       /* moving particles (-1 past nmoving) */
+  double disp[4][3];  /* their displacements */
+  double ds;          /* Action difference (both halves of the path for fixed node) */
+  double ds_node;     /* fixed-node (DoubleAction) difference */
+  int accepted;
+} pimc_displace_record;
+
+/* nattempt rigid-displacement attempts on every replica: DisplaceMoveSampler
+ * (src/advancer/DisplaceMoveSampler.cc:63-224), or DoubleDisplaceMoveSampler
+ * (src/advancer/DoubleDisplaceMoveSampler.cc:40-128) for fixed-node systems, with
+ * a UniformMover of box box[3] (src/advancer/UniformMover.cc:25-42), nmoving
+ * (1..4) particles chosen from all particles (species < 0) or from one
+ * species.  records: [nreplica][nattempt] or NULL. */
+int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmoving, int species,
+                      pimc_displace_record* records);
+
 /* ---- further estimators ------------------------------------------------- */
 
 /* Virial energy estimator with window nwindow (VirialEnergyEstimator,

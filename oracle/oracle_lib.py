@@ -380,6 +380,9 @@ class PortOracle(_Base):
             L.port_init_errors.argtypes = [C.c_void_p]
             L.port_ewald_long_range.restype = C.c_double
             L.port_ewald_long_range.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+            L.port_run_displace.argtypes = [C.c_void_p, C.c_int, C.c_uint32,
+                                            C.POINTER(C.c_double), C.c_int, C.c_int,
+                                            C.POINTER(OraDRecord)]
             L.port_virial_energy.restype = C.c_double
             L.port_virial_energy.argtypes = [C.c_void_p, C.c_int]
             L.port_coulomb_energy.restype = C.c_double
@@ -425,6 +428,7 @@ class PortOracle(_Base):
         self.h = C.c_void_p(L.port_create(C.byref(cfg), n, sp, tabs,
                                           C.byref(ew) if ew is not None else None))
         self._get, self._set, self._run = L.port_get_path, L.port_set_path, L.port_run
+        self._run_displace = L.port_run_displace
 
     def __del__(self):
         try:

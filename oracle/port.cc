@@ -1232,6 +1232,258 @@ struct Sim {
     return e / ns;
   }
   double charge(int ip) const { return cfg.spec_charge[spec[ip]]; }
+
+  // ---------------------------------------------------- rigid displacement
+  // SHOAction::getActionDifference(Paths, displacement, ...)
+  // (src/action/SHOAction.cc:107-143); the loop stops at the first moving
+  // particle outside the species, as the reference's `break` does.
+  double shoDisplaceDiff(int sp, const std::vector<int>& idx, const std::vector<V3>& disp,
+                         int i1, int i2) {
+    const double omega = cfg.sho_omega[sp], m = cfg.spec_mass[sp], tau = cfg.tau;
+    const double wt = omega * tau, sinhwt = sinh(wt), coshwt = cosh(wt);
+    const double div1 = 1.0 / (2.0 * sinhwt);
+    const int f = spec_first[sp], n = cfg.spec_count[sp];
+    double da = 0;
+    for (size_t k = 0; k < idx.size(); ++k) {
+      const int ip = idx[k];
+      if (ip < f || ip >= f + n) break;
+      for (int t = i1; t <= i2; ++t) {
+        double r1[3], r0[3];
+        for (int d = 0; d < 3; ++d) {
+          r1[d] = bead(ip, t).x[d];
+          r0[d] = bead(ip, t - 1).x[d];
+        }
+        da -= m * omega * ((dot3(r1, r1) + dot3(r0, r0)) * coshwt - 2.0 * dot3(r0, r1)) * div1;
+        for (int d = 0; d < 3; ++d) {
+          r1[d] += disp[k].x[d];
+          r0[d] += disp[k].x[d];
+        }
+        da += m * omega * ((dot3(r1, r1) + dot3(r0, r0)) * coshwt - 2.0 * dot3(r0, r1)) * div1;
+      }
+    }
+    return da;
+  }
+
+  // PairAction::getActionDifference(Paths, displacement, ...)
+  // (src/action/PairAction.cc:362-500), without the exchange correction.
+  double pairDisplaceDiff(const PairTab& pt, const std::vector<int>& idx,
+                          const std::vector<V3>& disp, int i1, int i2) {
+    double da = 0;
+    const int nmov = (int)idx.size();
+    for (int im = 0; im < nmov; ++im) {
+      const int i = idx[im];
+      int jb, je;
+      if (i >= pt.ifirst1 && i < pt.ifirst1 + pt.npart1) {
+        jb = pt.ifirst2;
+        je = pt.ifirst2 + pt.npart2;
+      } else if (i >= pt.ifirst2 && i < pt.ifirst2 + pt.npart2) {
+        jb = pt.ifirst1;
+        je = pt.ifirst1 + pt.npart1;
+      } else {
+        continue;
+      }
+      for (int j = jb; j < je; ++j) {
+        bool isMoving = false;
+        int jm = 0;
+        for (int k = 0; k < nmov; ++k)
+          if (j == idx[k]) {
+            isMoving = true;
+            jm = k;
+            break;
+          }
+        if (isMoving && i <= j) continue;
+        double prevDelta[3], pmd[3];
+        for (int d = 0; d < 3; ++d) prevDelta[d] = bead(i, i1 - 1).x[d] - bead(j, i1 - 1).x[d];
+        cell.pbc(prevDelta);
+        for (int d = 0; d < 3; ++d) {
+          pmd[d] = prevDelta[d] + disp[im].x[d];
+          if (isMoving) pmd[d] -= disp[jm].x[d];
+        }
+        cell.pbc(pmd);
+        double prevR = sqrt(dot3(prevDelta, prevDelta)), prevMovingR = sqrt(dot3(pmd, pmd));
+        for (int t = i1; t <= i2; ++t) {
+          double delta[3];
+          for (int d = 0; d < 3; ++d) {
+            delta[d] = bead(i, t).x[d] + disp[im].x[d] - bead(j, t).x[d];
+            if (isMoving) delta[d] -= disp[jm].x[d];
+          }
+          cell.pbc(delta);
+          double r = sqrt(dot3(delta, delta));
+          double q = 0.5 * (r + prevMovingR);
+          double action;
+          if (pt.norder > 0) {
+            double sv[3] = {delta[0] - pmd[0], delta[1] - pmd[1], delta[2] - pmd[2]};
+            action = pt.uk0(q, dot3(sv, sv) / (q * q));
+          } else {
+            action = pt.u00(q);
+          }
+          da += action;
+          for (int d = 0; d < 3; ++d) pmd[d] = delta[d];
+          prevMovingR = r;
+          for (int d = 0; d < 3; ++d) delta[d] = bead(i, t).x[d] - bead(j, t).x[d];
+          cell.pbc(delta);
+          r = sqrt(dot3(delta, delta));
+          q = 0.5 * (r + prevR);
+          if (pt.norder > 0) {
+            double sv[3] = {delta[0] - prevDelta[0], delta[1] - prevDelta[1],
+                            delta[2] - prevDelta[2]};
+            action = pt.uk0(q, dot3(sv, sv) / (q * q));
+          } else {
+            action = pt.u00(q);
+          }
+          da -= action;
+          for (int d = 0; d < 3; ++d) prevDelta[d] = delta[d];
+          prevR = r;
+        }
+      }
+    }
+    return da;
+  }
+
+  // CompositeAction::getActionDifference(Paths, displacement, ...) over
+  // Spring (0), SHO, PrimSHO (the base class's 0) and Coulomb (pairs, then the
+  // Ewald long range of every slice, src/action/CoulombAction.cc:123-146).
+  double actionDisplaceDiff(const std::vector<int>& idx, const std::vector<V3>& disp, int i1,
+                            int i2) {
+    double diff = 0;
+    for (int sp = 0; sp < cfg.nspecies; ++sp)
+      if (cfg.sho_omega[sp] > 0) diff += shoDisplaceDiff(sp, idx, disp, i1, i2);
+    if (cfg.coulomb) {
+      double u = 0;
+      for (size_t k = 0; k < pairs.size(); ++k) u += pairDisplaceDiff(pairs[k], idx, disp, i1, i2);
+      if (has_ewald) {
+        std::vector<V3> rew(np);
+        for (int t = i1; t <= i2; ++t) {
+          for (int p = 0; p < np; ++p) rew[p] = bead(p, t);
+          u -= ewald.evalLongRange(rew) * cfg.tau / cfg.epsilon;
+          for (size_t k = 0; k < idx.size(); ++k) {
+            for (int d = 0; d < 3; ++d) rew[idx[k]].x[d] += disp[k].x[d];
+            cell.pbc(rew[idx[k]].x);
+          }
+          u += ewald.evalLongRange(rew) * cfg.tau / cfg.epsilon;
+        }
+      }
+      diff += u;
+    }
+    return diff;
+  }
+
+  // FixedNodeAction::getActionDifference(Paths, displacement, ...)
+  // (src/fixednode/FixedNodeAction.cc:133-248) for one species' node model:
+  // new configuration (moving particles shifted on both slices of each pair)
+  // then the old one, slice pairs (t, t + M/2) for t in [i1, i2].
+  double nodeDisplaceDiff(int sp, const std::vector<int>& idx, const std::vector<V3>& disp,
+                          int i1, int i2) {
+    NodeModel& nm = nodes[sp];
+    const int f = spec_first[sp], n = cfg.spec_count[sp];
+    for (size_t i = 0; i < idx.size(); ++i) {
+      if (idx[i] >= f && idx[i] < f + n) break;
+      if (i == idx.size() - 1) return 0;
+    }
+    const int half = ns / 2;
+    std::vector<double> d1(np), d2(np), p1(np), p2(np);
+    std::vector<V3> r1(np), r2(np);
+    double da = 0, oldDet = 0;
+    for (int t = i1; t <= i2; ++t) {
+      for (int i = 0; i < np; ++i) {
+        r1[i] = bead(i, t);
+        r2[i] = bead(i, t + half);
+      }
+      for (size_t k = 0; k < idx.size(); ++k) {
+        for (int d = 0; d < 3; ++d) {
+          r1[idx[k]].x[d] += disp[k].x[d];
+          r2[idx[k]].x[d] += disp[k].x[d];
+        }
+        cell.pbc(r1[idx[k]].x);
+        cell.pbc(r2[idx[k]].x);
+      }
+      double det = 0;
+      if (nm.evaluate(r1, r2, 0, false, &det)) return 2e100;
+      if (t == i1) oldDet = det;
+      if (det * oldDet < 0.0) return 2e100;
+      nm.distance(r1, r2, 0, d1.data(), d2.data(), np);
+      if (t > i1)
+        for (int i = 0; i < np; ++i) da -= log((1 - exp(-d1[i] * p1[i])) * (1 - exp(-d2[i] * p2[i])));
+      p1 = d1;
+      p2 = d2;
+    }
+    for (int t = i1; t <= i2; ++t) {
+      for (int i = 0; i < np; ++i) {
+        r1[i] = bead(i, t);
+        r2[i] = bead(i, t + half);
+      }
+      double det = 0;
+      if (nm.evaluate(r1, r2, 0, false, &det)) return 2e100;
+      nm.distance(r1, r2, 0, d1.data(), d2.data(), np);
+      if (t > i1)
+        for (int i = 0; i < np; ++i) da += log((1 - exp(-d1[i] * p1[i])) * (1 - exp(-d2[i] * p2[i])));
+      p1 = d1;
+      p2 = d2;
+    }
+    return da;
+  }
+
+  // One DisplaceMoveSampler::run with nrepeat 1 (DoubleDisplaceMoveSampler for
+  // fixed-node systems): SimpleParticleChooser (species < 0) or
+  // SpeciesParticleChooser, UniformMover::makeMove (src/advancer/UniformMover.cc:25-42),
+  // tryMove (src/advancer/DisplaceMoveSampler.cc:158-224,
+  // DoubleDisplaceMoveSampler.cc:40-128).
+  bool displaceMove(uint32_t a, const double* dist, int nmoving, int species, ora_drecord* rec) {
+    attempt = a;
+    uidx = 0;
+    npair = 0;
+    ora_drecord dummy;
+    if (!rec) rec = &dummy;
+    memset(rec, 0, sizeof(*rec));
+    std::vector<int> idx(nmoving);
+    for (int im = 0; im < nmoving;) {
+      int i;
+      if (species < 0) {
+        i = (int)(np * uniform());
+        if (i == np) continue;
+      } else {
+        const int nsp = cfg.spec_count[species], f = spec_first[species];
+        i = (int)(nsp * uniform() + f);
+        if (i == nsp + f) i = nsp + f - 1;
+      }
+      bool dup = false;
+      for (int jm = 0; jm < im; ++jm) dup |= idx[jm] == i;
+      if (!dup) idx[im++] = i;
+    }
+    std::vector<V3> disp(nmoving);
+    for (int k = 0; k < nmoving; ++k)
+      for (int d = 0; d < 3; ++d) disp[k].x[d] = uniform();
+    for (int k = 0; k < nmoving; ++k)
+      for (int d = 0; d < 3; ++d) {
+        disp[k].x[d] -= 0.5;
+        disp[k].x[d] *= dist[d];
+      }
+    const int i1 = 0, i2 = fixed_node ? ns / 2 - 1 : ns - 1;
+    double ds = actionDisplaceDiff(idx, disp, i1, i2);
+    if (fixed_node) ds += actionDisplaceDiff(idx, disp, i1 + ns / 2, i2 + ns / 2);
+    double dsn = 0;
+    if (fixed_node)
+      for (int sp = 0; sp < cfg.nspecies; ++sp)
+        if (nodes[sp].kind) dsn += nodeDisplaceDiff(sp, idx, disp, i1, i2);
+    for (int k = 0; k < nmoving && k < ORA_MAX_MOVING; ++k) {
+      rec->ipart[k] = idx[k];
+      for (int d = 0; d < 3; ++d) rec->disp[k][d] = disp[k].x[d];
+    }
+    rec->ds = ds;
+    rec->ds_node = dsn;
+    const double acceptProb = exp(-(ds + dsn) + 0.0);
+    if (uniform() > acceptProb) return false;
+    rec->accepted = 1;
+    for (int t = i1; t <= i2; ++t)
+      for (int k = 0; k < nmoving; ++k) {
+        for (int half = 0; half < (fixed_node ? 2 : 1); ++half) {
+          V3& b = P(t + half * (ns / 2), idx[k]);
+          for (int d = 0; d < 3; ++d) b.x[d] += disp[k].x[d];
+          cell.pbc(b.x);
+        }
+      }
+    return true;
+  }
 };
 
 }  // namespace
@@ -1239,6 +1491,8 @@ struct Sim {
 extern "C" {
 
 double port_virial_energy(void* h, int nwindow);
+int port_run_displace(void* h, int n, uint32_t first_attempt, const double* dist, int nmoving,
+                      int species, ora_drecord* recs);
 double port_coulomb_energy(void* h, double epsilon);
 double port_ewald_coulomb_energy(void* h, double epsilon, double rcut, const ora_ewald_table* est,
                                  const double* vgrid);
@@ -1375,6 +1629,15 @@ int port_run(void* h, int n, uint32_t first_attempt, ora_record* recs) {
 }
 
 double port_thermo_energy(void* h) { return ((Sim*)h)->thermoEnergy(); }
+int port_run_displace(void* h, int n, uint32_t first_attempt, const double* dist, int nmoving,
+                      int species, ora_drecord* recs) {
+  Sim* s = (Sim*)h;
+  int nacc = 0;
+  for (int a = 0; a < n; ++a)
+    nacc += s->displaceMove(first_attempt + (uint32_t)a, dist, nmoving, species,
+                            recs ? &recs[a] : nullptr);
+  return nacc;
+}
 double port_virial_energy(void* h, int nwindow) { return ((Sim*)h)->virialEnergy(nwindow); }
 double port_coulomb_energy(void* h, double epsilon) { return ((Sim*)h)->coulombEnergy(epsilon); }
 double port_ewald_coulomb_energy(void* h, double epsilon, double rcut, const ora_ewald_table* est,

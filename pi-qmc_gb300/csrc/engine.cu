@@ -14,6 +14,7 @@
 #include "entry_kernels.cuh"
 #include "kernels.cuh"
 #include "noalloc_kernel.cuh"
+#include "displace_kernel.cuh"
 
 namespace pimc {
 // register-budget variants of the section kernel (section_variants.cu)
@@ -124,6 +125,7 @@ struct pimc_engine {
   int nactive = 0;
   // energy measurement buffers and captured step graphs
   DevBuf<double> d_partial;  // [nrep][kThermoChunks]
+  DevBuf<double> d_dscratch;  // displacement moves: node dets and distances per CTA
   DevBuf<double> d_energy;   // [steps][nrep]
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -141,6 +143,7 @@ struct pimc_engine {
     if (graph) cudaGraphExecDestroy(graph);
     if (cap_stream) cudaStreamDestroy(cap_stream);
     d_partial.free();
+    d_dscratch.free();
     d_energy.free();
     d_sys.free();
     d_state.free();
@@ -837,6 +840,79 @@ int run_estimator(pimc_engine* e, int which, EstimatorParams P, const Layout& L,
   return PIMC_OK;
 }
 }  // namespace
+
+int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmoving, int species,
+                      pimc_displace_record* records) {
+  if (!e || e->server || nattempt < 0 || !box || nmoving < 1 || nmoving > kMaxMoving)
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  for (const DevSys& d : e->hsys) {
+    if (species >= d.nspecies) return fail(PIMC_ERR_INVALID, "species out of range");
+    const int pool = species < 0 ? d.npart : d.spec_count[species];
+    if (nmoving > pool) return fail(PIMC_ERR_INVALID, "more moving particles than candidates");
+    if (d.fixed_node && (d.nslice % 2)) return fail(PIMC_ERR_INVALID, "odd nslice");
+  }
+  if (nattempt == 0) return PIMC_OK;
+  // shared memory: the section layout (slices staged for the Ewald sums, the
+  // reduction buffer, charges, control words, Slater scratch) plus a slice-pair
+  // staging area per lane group
+  const int nwarps = e->block / 32;
+  int stage = 0, half_max = 1, nsm = 1;
+  for (const DevSys& d : e->hsys) {
+    half_max = std::max(half_max, d.nslice / 2);
+    nsm = std::max(nsm, d.ns_max);
+    for (int i = 0; i < d.nspecies; ++i)
+      if (d.node_kind[i]) {
+        const int n = d.spec_count[i];
+        stage = std::max(stage, (32 / node_group_width(n)) * 6 * n);
+      }
+  }
+  const Layout L = e->lay;
+  const int stage_off = L.total;
+  const size_t smem = (size_t)(L.total + nwarps * stage) * 8;
+  if (smem > 200 * 1024) return fail(PIMC_ERR_CAPACITY, "displacement working set too large");
+  const long long sstride = (long long)half_max * (1 + 4 * nsm);
+  const size_t need = (size_t)e->grid * sstride;
+  if (e->d_dscratch.n < need && e->d_dscratch.alloc(need))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc displacement scratch");
+  pimc_displace_record* d_rec = nullptr;
+  if (records) {
+    CU(cudaMallocAsync(&d_rec, sizeof(pimc_displace_record) * (size_t)e->nrep * nattempt,
+                       e->stream));
+    CU(cudaMemsetAsync(d_rec, 0, sizeof(pimc_displace_record) * (size_t)e->nrep * nattempt,
+                       e->stream));
+  }
+  DisplaceParams P;
+  P.sys = e->d_sys.p;
+  P.state = e->d_state.p;
+  P.paths = e->d_paths.p;
+  P.nodecache = e->d_nodecache.p;
+  P.scratch = e->d_dscratch.p;
+  P.scratch_stride = sstride;
+  P.nodescr_g = e->d_nodescr.p;
+  P.rec = d_rec;
+  P.order = e->d_order.p;
+  P.next = e->d_next.p;
+  P.nattempt = nattempt;
+  P.nrep = e->nrep;
+  P.seed = e->seed;
+  for (int d = 0; d < 3; ++d) P.box[d] = box[d];
+  P.nmoving = nmoving;
+  P.species = species;
+  P.lay = L;
+  P.stage_off = stage_off;
+  cudaFuncSetAttribute(displace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
+  displace_kernel<<<e->grid, e->block, smem, e->stream>>>(P);
+  e->launches++;
+  CU(cudaGetLastError());
+  if (records) {
+    CU(cudaMemcpyAsync(records, d_rec, sizeof(pimc_displace_record) * (size_t)e->nrep * nattempt,
+                       cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaFreeAsync(d_rec, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+  }
+  return PIMC_OK;
+}
 
 int pimc_virial_energy(pimc_engine* e, int nwindow, double* host_energy) {
   if (!e || e->server || nwindow < 1 || !host_energy) return fail(PIMC_ERR_INVALID, "bad argument");

@@ -347,11 +347,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
           SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, k, -1, 0, 0, 0};
           double d = 0;
           int e2 = 0;
-          double* ec = (sho && mine) ? m.ecache + (size_t)k * n * n : nullptr;
-          if (!m.ecache) ec = nullptr;
           node_eval_dispatch(W, s, sp, v1, v2, sc2, dsc, mine ? 1 : 0, nullptr, -1, g == 0, d,
                              e2, m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm);
-          (void)ec;
           det = __shfl_sync(0xffffffffu, d, 0);
           err = __shfl_sync(0xffffffffu, e2, 0);
         }

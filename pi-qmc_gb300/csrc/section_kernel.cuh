@@ -584,7 +584,7 @@ static __device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipar
                                  double& enew) {
   const int np = s.npart;
   const int kx0 = s.ikmax[0], ky0 = s.ikmax[1], kz0 = s.ikmax[2];
-  const int nx = kx0 + 1, ny = 2 * ky0 + 1, nz = 2 * kz0 + 1;
+  const int nx = kx0 + 1, ny = 2 * ky0 + 1;
   double2* X = (double2*)m.ewt;        // [nx][np+1], column np = moved bead
   double2* Y = X + nx * (np + 1);      // [ny][np+1]
   double2* Z = Y + ny * (np + 1);      // [nz][np+1]

@@ -62,6 +62,11 @@ class LaunchConfig(C.Structure):
                 "ms": round(float(self.ms), 4)}
 
 
+class DisplaceRecord(C.Structure):
+    _fields_ = [("ipart", C.c_int * 4), ("disp", (C.c_double * 3) * 4), ("ds", C.c_double),
+                ("ds_node", C.c_double), ("accepted", C.c_int)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int), ("hbm_bytes", C.c_size_t), ("max_npart", C.c_int),
                 ("max_nslice", C.c_int), ("max_level", C.c_int), ("max_node_count", C.c_int)]
@@ -133,6 +138,7 @@ def lib():
         L.pimc_thermo_energy.argtypes = [P, D]
         L.pimc_run_steps.argtypes = [P, I, I, D]
         L.pimc_virial_energy.argtypes = [P, I, D]
+        L.pimc_run_displace.argtypes = [P, I, D, I, I, C.POINTER(DisplaceRecord)]
         L.pimc_coulomb_energy.argtypes = [P, C.c_double, D]
         L.pimc_ewald_coulomb_energy.argtypes = [P, C.c_double, C.c_double,
                                                 C.POINTER(EwaldTable), D, D]
@@ -360,6 +366,26 @@ class Engine:
         cfg = LaunchConfig()
         _check(lib().pimc_engine_get_config(self.h, C.byref(cfg)))
         return cfg.as_dict()
+
+    def run_displace(self, nattempt, box, nmoving=1, species=-1, records=False):
+        """nattempt rigid-displacement attempts per replica (uniform box[3])."""
+        b = np.ascontiguousarray(box, np.float64)
+        if records:
+            n = self.nreplica * nattempt
+            recs = (DisplaceRecord * max(n, 1))()
+            _check(lib().pimc_run_displace(self.h, nattempt, _dp(b), nmoving, species, recs))
+            out = {
+                "ipart": np.array([[recs[i].ipart[k] for k in range(nmoving)] for i in range(n)],
+                                  np.int32),
+                "disp": np.array([[list(recs[i].disp[k]) for k in range(nmoving)]
+                                  for i in range(n)]),
+                "ds": np.array([recs[i].ds for i in range(n)]),
+                "ds_node": np.array([recs[i].ds_node for i in range(n)]),
+                "accepted": np.array([recs[i].accepted for i in range(n)], np.int32),
+            }
+            return {k: v.reshape((self.nreplica, nattempt) + v.shape[1:]) for k, v in out.items()}
+        _check(lib().pimc_run_displace(self.h, nattempt, _dp(b), nmoving, species, None))
+        return None
 
     def replica_status(self):
         n = self.nreplica

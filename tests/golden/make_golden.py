@@ -8,7 +8,9 @@ level, per-level action differences and mover log transition ratios), the
 final path (stored as its difference from the initial path, which compresses)
 and, on the final path, the thermodynamic, virial (windows 1, 4, 16) and
 Coulomb energy estimators (direct, and for periodic cases the optimized-Ewald
-estimator together with the Ewald table and short-range grid it built).
+estimator together with the Ewald table and short-range grid it built), and
+for some cases a recorded run of rigid-displacement moves from the final path
+(DisplaceMoveSampler / DoubleDisplaceMoveSampler with a UniformMover).
 
 The fixtures let machines without the reference tree (the GPU machine) pin the C++
 restatement and the CUDA engine against the reference's own outputs.
@@ -30,6 +32,14 @@ import workloads as W  # noqa: E402
 
 
 VIRIAL_WINDOWS = (1, 4, 16)
+# rigid-displacement runs from the final path: (box, nmoving, species, attempts)
+DISPLACE = {
+    "dot2_small": ((0.5, 0.5, 0.5), 1, -1, 60),
+    "dot2_full": ((0.6, 0.4, 0.5), 2, -1, 40),
+    "dot4_fn": ((0.3, 0.3, 0.3), 2, 1, 40),
+    "heg8": ((1.0, 1.0, 1.0), 1, -1, 30),
+}
+
 
 
 def run_case(name, kw, init, nattempt):
@@ -77,6 +87,14 @@ def run_case(name, kw, init, nattempt):
         out["estew_ikmax"] = np.array(est["ikmax"], np.int32)
         out["estew_vgrid"] = vg
         out["est_ewald_coulomb"] = np.array(ref.ewald_coulomb_energy(1.0, rcut, kcut))
+    if name in DISPLACE:
+        box, nmov, species, nd = DISPLACE[name]
+        # the chain continues: attempt numbers follow the section attempts
+        d = ref.run_displace(nd, box, nmov, species, first_attempt=nattempt)
+        out["disp_params"] = np.array([box[0], box[1], box[2], nmov, species, nd, nattempt])
+        for k in ("ipart", "disp", "ds", "ds_node", "accepted"):
+            out["disp_" + k] = d[k]
+        out["disp_dpath"] = ref.get_path() - x1
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print(f"{name}: {nattempt} attempts, {recs['naccepted']} accepted, "

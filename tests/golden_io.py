@@ -39,7 +39,15 @@ def load(name):
                                        self_energy=float(z["estew_scalars"][1]),
                                        ikmax=[int(v) for v in z["estew_ikmax"]]),
                             vgrid=z["estew_vgrid"], energy=float(z["est_ewald_coulomb"]))
-    return dict(kw=kw, tables=tabs, ewald=ew, path0=z["path0"], estimators=est,
+    disp = None
+    if "disp_params" in z:
+        prm = z["disp_params"]
+        disp = dict(box=[float(v) for v in prm[:3]], nmoving=int(prm[3]), species=int(prm[4]),
+                    nattempt=int(prm[5]), first_attempt=int(prm[6]),
+                    records={k: z["disp_" + k] for k in ("ipart", "disp", "ds", "ds_node",
+                                                         "accepted")},
+                    path=z["path0"] + z["dpath"] + z["disp_dpath"])
+    return dict(kw=kw, tables=tabs, ewald=ew, path0=z["path0"], estimators=est, displace=disp,
                 path1=z["path0"] + z["dpath"], energy0=float(z["energy0"]),
                 energy1=float(z["energy1"]), records=rec, nattempt=int(z["nattempt"]),
                 naccepted=int(z["naccepted"]))

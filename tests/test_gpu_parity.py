@@ -307,3 +307,25 @@ def test_estimators_match_golden(pimc, case):
         x = est["ewald"]
         got = e.ewald_coulomb_energy(x["epsilon"], x["rcut"], x["table"], x["vgrid"])
         assert np.allclose(got, x["energy"], rtol=1e-11), (got, x["energy"])
+
+
+@pytest.mark.parametrize("case", ["dot2_small", "dot2_full", "dot4_fn", "heg8"])
+def test_displace_matches_golden(pimc, case):
+    # Rigid displacement moves through the ABI from the final golden path, against
+    # pi-qmc's DisplaceMoveSampler / DoubleDisplaceMoveSampler: particles,
+    # displacements and decisions exact, action differences 1e-11 (the engine
+    # sums slices and pairs in parallel), node terms 1e-9, final path 1e-12.
+    g = golden_io.load(case)
+    d = g["displace"]
+    e = engine_for(pimc, g)
+    e.upload_paths([g["path0"]])
+    e.run_sections(g["nattempt"])  # the golden section attempts (path0 -> path1)
+    assert d["first_attempt"] == g["nattempt"]
+    r = e.run_displace(d["nattempt"], d["box"], d["nmoving"], d["species"], records=True)
+    ref = d["records"]
+    assert np.array_equal(r["ipart"][0], ref["ipart"])
+    assert np.array_equal(r["disp"][0], ref["disp"])
+    assert np.array_equal(r["accepted"][0], ref["accepted"])
+    assert rel_close(r["ds"][0], ref["ds"], 1e-11)
+    assert rel_close(r["ds_node"][0], ref["ds_node"], 1e-9)
+    assert np.abs(e.download_paths()[0] - d["path"]).max() <= 1e-12

@@ -182,3 +182,23 @@ def test_estimator_ewald_builder_against_reference():
     port.set_path(g["path1"])
     got = port.ewald_coulomb_energy(e["epsilon"], e["rcut"], ew, vg)
     assert got == pytest.approx(e["energy"], rel=1e-3)
+
+
+@pytest.mark.parametrize("case", ["dot2_small", "dot2_full", "dot4_fn", "heg8"])
+def test_port_displace_matches_golden(case):
+    # Rigid displacement moves (DisplaceMoveSampler / DoubleDisplaceMoveSampler)
+    # from the final golden path: particles, displacements and decisions exact,
+    # action differences 1e-12 (node terms 1e-10), final path 1e-12.
+    g = golden_io.load(case)
+    d = g["displace"]
+    port = O.PortOracle(O.make_config(**g["kw"]), g["tables"], g["ewald"])
+    port.set_path(g["path1"])
+    r = port.run_displace(d["nattempt"], d["box"], d["nmoving"], d["species"],
+                          first_attempt=d["first_attempt"])
+    ref = d["records"]
+    assert np.array_equal(r["ipart"], ref["ipart"])
+    assert np.array_equal(r["accepted"], ref["accepted"])
+    assert np.array_equal(r["disp"], ref["disp"])
+    assert np.allclose(r["ds"], ref["ds"], rtol=1e-12, atol=1e-12)
+    assert np.allclose(r["ds_node"], ref["ds_node"], rtol=1e-10, atol=1e-10)
+    assert np.abs(port.get_path() - d["path"]).max() <= 1e-12
