@@ -98,6 +98,19 @@ def sweep_attempts(kw):
     return -(-kw["nslice"] // (1 << L)) * sum(kw["counts"])
 
 
+# ------------------------------------------------------- measured work per unit
+# Thread-level FP64 flops (DADD + DMUL + 2 DFMA, predicated-on lanes only) and
+# DRAM bytes (read + write) per section attempt of the section kernel, counted
+# by ncu on the same kernel and workload in the steady state (the timed sweep of
+# a 304-replica run after a warm-up sweep).  The commands and raw counts are in
+# profiles/fp64_work_per_attempt.md; they are the roofline numerator.
+MEASURED_WORK = {
+    # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
+    ("dot20_fn", "mixed"): (299983.4, None),
+    ("dot20_fn", "fp64"): (518953.4, None),
+}
+
+
 # ---------------------------------------------------------------- flop model
 def attempt_flops(kw, reach):
     """Algorithmic FP64 work of one section-move attempt (flops; an FMA is 2,
@@ -452,14 +465,35 @@ def run_engine(args, rank, world):
         torch.cuda.synchronize()
         plain_value = A * ((1 << L) - 1) / (a0.elapsed_time(a1) * 1e-3)
         plain.close()
-    # ---- roofline of the dominant kernel (the section-move kernel)
+    # ---- roofline of the dominant kernel (the section-move kernel), timed
+    # alone with CUDA events on its stream over three more launches
+    sec_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(3)]
+    torch.cuda.synchronize()
+    for a0, a1 in sec_ev:
+        flush.fill_(1.0)
+        a0.record(stream)
+        eng.run_sections(A)
+        a1.record(stream)
+    torch.cuda.synchronize()
+    section_ms = statistics.mean(a0.elapsed_time(a1) for a0, a1 in sec_ev)
     fp64_peak = pimc_gb300.fp64_peak_tflops()
-    if batch:
-        flops = sum(attempt_flops(k, [depth_reach[k["nlevel"] - lev]
-                                      for lev in range(k["nlevel"] + 1)]) for k in systems) * A
+    work = MEASURED_WORK.get((args.workload, args.precision))
+    if work is not None:
+        flops = work[0] * R * A
+        traffic = work[1] * R * A if work[1] is not None else None
+        flops_source = ("ncu thread-level DADD+DMUL+2*DFMA per attempt of this kernel and "
+                        "workload (profiles/fp64_work_per_attempt.md) x attempts per launch")
     else:
-        flops = attempt_flops(kw, reach) * R * A
-    achieved = flops / (t_ms / args.steps * 1e-3) / 1e12
+        if batch:
+            flops = sum(attempt_flops(k, [depth_reach[k["nlevel"] - lev]
+                                          for lev in range(k["nlevel"] + 1)])
+                        for k in systems) * A
+        else:
+            flops = attempt_flops(kw, reach) * R * A
+        traffic = None
+        flops_source = "operation-count model (bench.py attempt_flops); no ncu count yet"
+    achieved = flops / (section_ms * 1e-3) / 1e12
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
@@ -482,9 +516,11 @@ def run_engine(args, rank, world):
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                     "section_ms_per_launch": section_ms, "flops_per_launch": flops,
+                     "flops_source": flops_source,
                      "peak_source": "measured FP64 FMA probe (pimc_fp64_peak); "
                                     "MEASURED_PEAKS.json holds no FP64 figure",
-                     "traffic": None, "kernel": "section_moves_kernel",
+                     "traffic": traffic, "kernel": "section_moves_kernel",
                      "flops_per_attempt_model": attempt_flops(kw, reach),
                      "level_reach": reach},
         "clocks": clk.summary(),

@@ -221,7 +221,7 @@ int pimc_ewald_estimator_tables(const pimc_system* sys, double rcut, double kcut
 /* ---- launch configuration and autotuning -------------------------------- */
 
 /* Launch configuration of an engine's section kernel: threads per replica
- * (64, 128 or 256), the per-warp Slater scratch in shared (0) or global (1)
+ * (64, 128, 256, or 512 with variant 1), the per-warp Slater scratch in shared (0) or global (1)
  * memory, the replicas resident per SM (0: as many as fit) and the section
  * kernel's register-budget variant.  ms is the
  * time the autotuner measured for it (0 when not measured).  A configuration
@@ -231,7 +231,8 @@ typedef struct {
   int block;
   int scratch_global;
   int ctas_per_sm;
-  int regs_variant;  /* register budget: 65536 / (256 * regs_variant) per thread (2, 3 or 4; 0 = 2) */
+  int regs_variant;  /* register budget: 65536 / (256 * regs_variant) per thread (2, 3 or 4;
+                        0 = 2), or 1: the variant for up to 512 threads (128 registers) */
   float ms;
 } pimc_launch_config;
 

@@ -18,12 +18,15 @@
 
 namespace pimc {
 // register-budget variants of the section kernel (section_variants.cu)
+cudaError_t section_launch_v1(int, int, size_t, cudaStream_t, const RunParams&);
 cudaError_t section_launch_v2(int, int, size_t, cudaStream_t, const RunParams&);
 cudaError_t section_launch_v3(int, int, size_t, cudaStream_t, const RunParams&);
 cudaError_t section_launch_v4(int, int, size_t, cudaStream_t, const RunParams&);
+int section_occupancy_v1(int, size_t);
 int section_occupancy_v2(int, size_t);
 int section_occupancy_v3(int, size_t);
 int section_occupancy_v4(int, size_t);
+void section_smem_cap_v1(int);
 void section_smem_cap_v2(int);
 void section_smem_cap_v3(int);
 void section_smem_cap_v4(int);
@@ -32,14 +35,17 @@ void section_smem_cap_v4(int);
 using namespace pimc;
 
 namespace {
-// minb: 2, 3 or 4 resident 256-thread blocks per SM worth of registers
+// minb: 2, 3 or 4 resident 256-thread blocks per SM worth of registers, or 1:
+// the 512-thread variant (128 registers)
 cudaError_t section_launch(int minb, int grid, int block, size_t smem, cudaStream_t st,
                            const RunParams& P) {
+  if (minb == 1) return section_launch_v1(grid, block, smem, st, P);
   if (minb == 3) return section_launch_v3(grid, block, smem, st, P);
   if (minb == 4) return section_launch_v4(grid, block, smem, st, P);
   return section_launch_v2(grid, block, smem, st, P);
 }
 int section_occupancy(int minb, int block, size_t smem) {
+  if (minb == 1) return section_occupancy_v1(block, smem);
   if (minb == 3) return section_occupancy_v3(block, smem);
   if (minb == 4) return section_occupancy_v4(block, smem);
   return section_occupancy_v2(block, smem);
@@ -370,6 +376,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
 }
 
 void set_smem_caps() {
+  section_smem_cap_v1(200 * 1024);
   section_smem_cap_v2(200 * 1024);
   section_smem_cap_v3(200 * 1024);
   section_smem_cap_v4(200 * 1024);
@@ -902,7 +909,7 @@ int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmovi
   P.stage_off = stage_off;
   cudaFuncSetAttribute(displace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  displace_kernel<<<e->grid, e->block, smem, e->stream>>>(P);
+  displace_kernel<<<e->grid, std::min(e->block, kBlock), smem, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
   if (records) {
@@ -1144,8 +1151,9 @@ int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
 // ------------------------------------------------- launch configuration
 namespace {
 int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int minb) {
-  if (block != 64 && block != 128 && block != 256) return fail(PIMC_ERR_INVALID, "block must be 64, 128 or 256");
-  if (minb < 2 || minb > 4) return fail(PIMC_ERR_INVALID, "register variant must be 2, 3 or 4");
+  if (minb < 1 || minb > 4) return fail(PIMC_ERR_INVALID, "register variant must be 1, 2, 3 or 4");
+  if (block != 64 && block != 128 && block != 256 && !(block == 512 && minb == 1))
+    return fail(PIMC_ERR_INVALID, "block must be 64, 128, 256 (or 512 with variant 1)");
   bool ok = false;
   const Layout L = make_layout(e->hsys, block / 32, ok, opts);
   if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
@@ -1221,6 +1229,7 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   for (int v : {2, 3, 4})
     for (int b : {64, 128, 256})
       for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
+  for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({512, g, 0, 1, 0.f});
   cudaEvent_t t0, t1;
   CU(cudaEventCreate(&t0));
   CU(cudaEventCreate(&t1));

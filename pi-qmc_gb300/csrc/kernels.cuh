@@ -455,11 +455,11 @@ __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int leve
   return u;
 }
 
-// MINB sets the register budget (65536 / (kBlock * MINB) per thread); the
-// variants are compiled in separate translation units (section_variants.cu)
-// and chosen at run time by the launch configuration.
-template <int MINB>
-__global__ void __launch_bounds__(kBlock, MINB) section_moves_kernel(RunParams P) {
+// NT (largest block) and MINB set the register budget, 65536 / (NT * MINB)
+// per thread; the variants are compiled in separate translation units
+// (section_variants.cu) and chosen at run time by the launch configuration.
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
   extern __shared__ double smem[];
   __shared__ DevSys S;
   __shared__ double scale[kMaxSpecies];

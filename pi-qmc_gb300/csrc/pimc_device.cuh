@@ -12,8 +12,9 @@ constexpr int kMaxSpecies = 4;
 constexpr int kMaxTables = 10;
 constexpr int kMaxNs = 32;  // particles per node-model species
 constexpr int kMaxLevels = 8;  // levels 0..nlevel+1
-constexpr int kBlock = 256;    // largest block; engines pick 64..256 threads
-constexpr int kWarps = kBlock / 32;
+constexpr int kBlock = 256;     // threads of the estimator and entry-point kernels
+constexpr int kMaxBlock = 512;  // largest section-kernel block (64..512 threads)
+constexpr int kWarps = kMaxBlock / 32;  // reduction slots
 
 struct DevTable {
   const double* ugrid;  // (ngpts,2,ndata)

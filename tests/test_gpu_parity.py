@@ -234,7 +234,7 @@ def test_graph_steps_equal_direct_calls(pimc):
 
 @pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small"])
 @pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 4), (128, 1, 3), (256, 1, 2),
-                                                       (256, 0, 3)])
+                                                       (256, 0, 3), (512, 1, 1), (512, 0, 1)])
 def test_launch_configs_match_golden(pimc, case, block, scratch_global, regs):
     # Every launch configuration the autotuner may pick reproduces pi-qmc's
     # decisions and action differences.
@@ -279,7 +279,7 @@ def test_register_variants_bit_identical(pimc):
     # same results bit for bit.
     g = golden_io.load("dot4_fn")
     out = []
-    for regs in (2, 3, 4):
+    for regs in (2, 3, 4, 1):
         e = engine_for(pimc, g, nreplica=4)
         e.configure(256, 0, 0, regs)
         e.upload_paths([g["path0"]] * 4)
