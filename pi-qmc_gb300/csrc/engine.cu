@@ -325,6 +325,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.s1 = take(3 * nsec * np);
   L.s2 = take(fixed ? 3 * nsec * np : 0);
   L.mv = take(3 * nsec);
+  L.nrm = take(3 * nsec);
   L.red = take(64);
   L.q = take(np);
   L.dm = take(kMaxSpecies * nsec);
@@ -408,6 +409,7 @@ Layout estimator_layout(const std::vector<DevSys>& sys, const int* ikmax_extra) 
   L.s1 = take(3 * nsec * np);
   L.s2 = L.s1;
   L.mv = take(3 * nsec);
+  L.nrm = L.mv;
   L.red = take(64);
   L.q = take(np);
   L.ewt = take(2 * ((ik[0] + 1) + (2 * ik[1] + 1) + (2 * ik[2] + 1)) * (np + 1));

@@ -11,6 +11,7 @@ namespace pimc {
 struct Layout {
   int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
   int ncol_stride;
+  int nrm;  // the attempt's normals, 3 per movable slice
   int nodescr_in_smem;
   int nodescr_stride;
   int total;  // doubles
@@ -56,6 +57,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.ictl = (int*)(base + L.ictl);
   m.ecache = L.ecache >= 0 ? base + L.ecache : nullptr;
   m.ncol = L.ncol >= 0 ? base + L.ncol : nullptr;
+  m.nrm = base + L.nrm;
   m.ncol_stride = L.ncol_stride;
   m.nodescr_stride = L.nodescr_stride;
   m.nodescr = L.nodescr_in_smem
@@ -109,6 +111,32 @@ static __device__ void store_section(const DevSys& s, double* path, int ifirst, 
 // FreeMover::makeMove (src/advancer/mover/FreeMover.cc:59-124) and
 // FreeMoverPBC::makeMove (src/advancer/mover/FreeMoverPBC.cc:59-152) for one
 // moving particle at one level; threads own moved slices.  Returns ln(T_old/T_new).
+// Every normal the attempt's mover can use, drawn in parallel before the
+// levels: moved slice `ord` (0 .. 2^L - 2 in FreeMover's order) takes Box-Muller
+// pairs 2 ord and 2 ord + 1 and uses the first three values (FP32 transform
+// in the mixed form).
+static __device__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t seed,
+                                       uint32_t rep, uint32_t att) {
+  const int nord = (1 << s.nlevel) - 1;
+  for (int o = threadIdx.x; o < nord; o += blockDim.x) {
+    double z0, z1, z2, z3;
+    if (s.mixed) {
+      float f0, f1, f2, f3;
+      stream_normal_pair_f(seed, rep, att, 2u * o, &f0, &f1);
+      stream_normal_pair_f(seed, rep, att, 2u * o + 1u, &f2, &f3);
+      z0 = f0;
+      z1 = f1;
+      z2 = f2;
+    } else {
+      stream_normal_pair(seed, rep, att, 2u * o, &z0, &z1);
+      stream_normal_pair(seed, rep, att, 2u * o + 1u, &z2, &z3);
+    }
+    m.nrm[3 * o] = z0;
+    m.nrm[3 * o + 1] = z1;
+    m.nrm[3 * o + 2] = z2;
+  }
+}
+
 static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
                               uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
   const int L = s.nlevel, np = s.npart;
@@ -121,19 +149,9 @@ static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, 
   double part = 0.0;
   for (int k = threadIdx.x; k < nmov; k += blockDim.x) {
     const int t = nStride * (2 * k + 1), tp = t - nStride, tn = t + nStride;
-    double z0, z1, z2, z3;
-    if (s.mixed) {
-      float f0, f1, f2, f3;
-      stream_normal_pair_f(seed, rep, att, 2u * (ord0 + k), &f0, &f1);
-      stream_normal_pair_f(seed, rep, att, 2u * (ord0 + k) + 1u, &f2, &f3);
-      z0 = f0;
-      z1 = f1;
-      z2 = f2;
-      z3 = f3;
-    } else {
-      stream_normal_pair(seed, rep, att, 2u * (ord0 + k), &z0, &z1);
-      stream_normal_pair(seed, rep, att, 2u * (ord0 + k) + 1u, &z2, &z3);
-    }
+    // the attempt's normals were drawn up front (attempt_normals)
+    const double z0 = m.nrm[3 * (ord0 + k)], z1 = m.nrm[3 * (ord0 + k) + 1];
+    const double z2 = m.nrm[3 * (ord0 + k) + 2];
     const double ox = m.s1x[t * np + ipart], oy = m.s1y[t * np + ipart], oz = m.s1z[t * np + ipart];
     const double opx = m.s1x[tp * np + ipart], opy = m.s1y[tp * np + ipart], opz = m.s1z[tp * np + ipart];
     const double onx = m.s1x[tn * np + ipart], ony = m.s1y[tn * np + ipart], onz = m.s1z[tn * np + ipart];
@@ -279,8 +297,11 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
       }
       __syncthreads();
       const int nmiss = m.ictl[C_NMISS];
-      for (int base = warp * G; base < nmiss; base += nwarps * G) {
-        const int task = base + g;
+      // warp-wide lane groups when the misses do not fill the warps
+      const int Wm = nmiss <= nwarps ? 32 : W, Gm = 32 / Wm, gm = lane / Wm, glm = lane & (Wm - 1);
+      double* scrm = m.nodescr + (size_t)warp * m.nodescr_stride + gm * node_group_scratch(n, !sho);
+      for (int base = warp * Gm; base < nmiss; base += nwarps * Gm) {
+        const int task = base + gm;
         const bool act = task < nmiss;
         const int t = miss[act ? task : base];
         double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
@@ -294,13 +315,13 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
         const int full = (mine || e) ? 1 : 0;
         double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
         double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
-        node_eval_dispatch(W, s, sp, v1, v2, sc, scr, full, ec, -1, act, det, err, d1, d2);
+        node_eval_dispatch(Wm, s, sp, v1, v2, sc, scrm, full, ec, -1, act, det, err, d1, d2);
         if (act) {
-          if (e && mine && gl < n) {
-            e[2 + gl] = d1[gl];
-            e[2 + n + gl] = d2[gl];
+          if (e && mine && glm < n) {
+            e[2 + glm] = d1[glm];
+            e[2 + n + glm] = d2[glm];
           }
-          if (gl == 0) {
+          if (glm == 0) {
             m.edet[t] = det;
             errs[t] = err;
             if (e) {
@@ -388,13 +409,27 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
   const int nsec = s.nsec, nsm = s.ns_max;
   const int nStride = 1 << (level + 1);
   const int n = s.spec_count[msp];
-  const int W = node_group_width(n), G = 32 / W, g = lane / W;
+  const int ntask = (nsec - 1 - nStride / 2) / nStride + 1;
+  if (nStride / 2 == nsec - 1) {
+    // The top level's only slice is the section's fixed end: its Slater
+    // matrix is the set-up one, so its determinant and distances are copied.
+    const int t = nsec - 1;
+    for (int i = threadIdx.x; i < 2 * nsm; i += blockDim.x) m.ndist[t * 2 * nsm + i] = m.dist[t * 2 * nsm + i];
+    if (threadIdx.x == 0) {
+      m.ndm[t] = m.dm[msp * nsec + t];
+      m.ictl[C_FLAG] = (m.ndm[t] * m.dm[msp * nsec + 0] <= 1e-200) ? 1 : 0;
+    }
+    __syncthreads();
+    return m.ictl[C_FLAG] ? 2e100 : 0.0;
+  }
+  // lane groups as wide as the warp when the tasks do not fill the warps
+  // (the evaluation is the same, element for element, at any width)
+  const int W = ntask <= nwarps ? 32 : node_group_width(n), G = 32 / W, g = lane / W;
   const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
   double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
   const int jcol = ipart - s.spec_first[msp];
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
-  const int ntask = (nsec - 1 - nStride / 2) / nStride + 1;
   for (int base = warp * G; base < ntask; base += nwarps * G) {
     const int task = base + g;
     const bool act = task < ntask;
@@ -530,6 +565,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       const int ipart = m.ictl[C_IPART];
       load_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
       if (s.fixed_node) load_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+      attempt_normals(s, m, P.seed, s.stream_id, att);
       __syncthreads();
       for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
         m.mx[t] = m.s1x[t * np + ipart];

@@ -35,6 +35,7 @@ struct Smem {
   double* ecache;           // [nsec][n*n] exp matrices of the moving species (SHONodes)
   double* ncol;             // [nsec][ncol_stride] recomputed column of each changed slice
   int ncol_stride;          // ns_max (SHO exp column) or 4 ns_max (free-particle values + gradients)
+  double* nrm;              // [2^L - 1][3] the attempt's proposal normals
   int nodescr_stride;       // doubles per warp
 };
 
