@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(kBlock) action_diff_kernel(ActionDiffParams P)
   for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
   __syncthreads();
   const int ip = P.ipart[b];
-  double ds = block_sum(action_partial(s, m, ip, P.level), m.red);
+  double ds = block_sum(action_partial(s, m, ip, P.level, threadIdx.x, blockDim.x), m.red);
   if (s.ewald && s.coulomb && P.level == 0)
     for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ip, t);
   if (threadIdx.x == 0) P.ds[b] = ds;

@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       for (int level = L; level >= 0; --level) {
         const uint32_t ubase = level_uniform_base(s, level);
         const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
-        double ds = block_sum(action_partial(s, m, ipart, level), m.red);
+        double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
         if (s.ewald && s.coulomb && level == 0) {
           for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
         }

@@ -417,7 +417,8 @@ static __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& 
 // (src/action/PrimSHOAction.cc:21-58), PairAction per species pair
 // (src/action/PairAction.cc:219-360).  Work items are links and (partner, link)
 // pairs; each item contributes (new - old).
-static __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level) {
+static __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level,
+                                        int tid, int nthreads) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
   const int nlinks = 1 << (L - level);
@@ -452,7 +453,7 @@ static __device__ double action_partial(const DevSys& s, const Smem& m, int ipar
   }
   int total = nlinks;
   for (int q = 0; q < nt; ++q) total += tn[q] * nlinks;
-  for (int item = threadIdx.x; item < total; item += blockDim.x) {
+  for (int item = tid; item < total; item += nthreads) {
     if (item < nlinks) {
       const int k = item + 1;
       const int t1 = k * nStride, t0 = t1 - nStride;
