@@ -378,7 +378,7 @@ def run_engine(args, rank, world):
     host = torch.from_numpy(paths).pin_memory()
     eng.upload_paths(paths)
     # launch configuration chosen by the autotuner (untimed; the chains are restored)
-    tuned, tried = eng.autotune(min(A, 16)) if not args.no_autotune else (eng.launch_config(), [])
+    tuned, tried = eng.autotune(min(A, 32)) if not args.no_autotune else (eng.launch_config(), [])
     # depth statistics for the flop model (untimed)
     rec = eng.run_sections(4, records=True)
     # fraction of attempts that evaluate each level, by depth below the top level

@@ -409,6 +409,18 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
               }
       }
       __syncthreads();
+      if (m.ictl[C_REJECT] == 0 && dbl && cache) {
+        // the species' cached element matrices are stale in rows and columns
+        for (int sp = 0; sp < s.nspecies; ++sp) {
+          bool any = false;
+          for (int k = 0; k < nmov; ++k)
+            any |= mov[k] >= s.spec_first[sp] && mov[k] < s.spec_first[sp] + s.spec_count[sp];
+          if (!any || !s.node_kind[sp]) continue;
+          const int ms = cache_mask_slot(s, sp);
+          for (int t = threadIdx.x; t < M; t += blockDim.x)
+            cache_entry(s, cache, sp, t)[ms] = __longlong_as_double(-1ll);
+        }
+      }
       if (m.ictl[C_REJECT] == 0) {
         for (int it = threadIdx.x; it < nmov * M; it += blockDim.x) {
           const int k = it / M, t = it % M;

@@ -232,16 +232,29 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
                                                    double scale, double* scr, int full,
                                                    double* ecache, int jcol, bool write,
                                                    double& det, int& err, double* d1,
-                                                   double* d2, double* newcol = nullptr) {
+                                                   double* d2, double* newcol = nullptr,
+                                                   unsigned rowmask = 0xffffffffu) {
   if (W == 8)
     node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                       newcol);
+                       newcol, rowmask);
   else if (W == 16)
     node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                        newcol);
+                        newcol, rowmask);
   else
     node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                        newcol);
+                        newcol, rowmask);
+}
+
+// Index of the entry's stale-row word (after the element matrices): bit r set
+// = row r (r2 particle r) moved since the matrix was cached; bit 63 = the
+// cached matrix is not usable at all.
+__device__ __forceinline__ int cache_mask_slot(const DevSys& s, int sp) {
+  const int n = s.spec_count[sp];
+  return 2 + 2 * n + n * n * (s.node_kind[sp] == PIMC_NODES_FREE ? 4 : 1);
+}
+__device__ __forceinline__ unsigned cache_rowmask(const double* e, int slot) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(e[slot]);
+  return (b >> 63) ? 0xffffffffu : (unsigned)(b & 0xffffffffull);
 }
 
 // Slater-result cache entry of species sp for path slice t1 (r1 at t1, r2 at
@@ -315,7 +328,9 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
         const int full = (mine || e) ? 1 : 0;
         double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
         double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
-        node_eval_dispatch(Wm, s, sp, v1, v2, sc, scrm, full, ec, -1, act, det, err, d1, d2);
+        const unsigned rmask = e ? cache_rowmask(e, cache_mask_slot(s, sp)) : 0xffffffffu;
+        node_eval_dispatch(Wm, s, sp, v1, v2, sc, scrm, full, ec, -1, act, det, err, d1, d2,
+                           nullptr, rmask);
         if (act) {
           if (e && mine && glm < n) {
             e[2 + glm] = d1[glm];
@@ -327,6 +342,7 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
             if (e) {
               e[1] = det;
               e[0] = err ? NaN : ep;
+              e[cache_mask_slot(s, sp)] = 0.0;  // the element matrix is whole again
             }
           }
         }
@@ -445,7 +461,7 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
       ec = m.ecache + (size_t)t * n * n;
     node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
                        m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                       cache ? m.ncol + t * m.ncol_stride : nullptr);
+                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u);
     if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
@@ -641,7 +657,10 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
             double* e = cache_entry(s, cache, msp, t1);
             e[1] = m.ndm[k];
             e[0] = (double)epoch[msp];
-            cache_entry(s, cache, msp, (t1 + M / 2) % M)[0] = NaN;
+            double* o = cache_entry(s, cache, msp, (t1 + M / 2) % M);
+            o[0] = NaN;
+            const int ms = cache_mask_slot(s, msp);
+            o[ms] = __longlong_as_double(__double_as_longlong(o[ms]) | (1ll << jcol));
           }
         }
       }

@@ -87,7 +87,7 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
                                 int& err_out, double* d1, double* d2,
-                                double* newcol = nullptr) {
+                                double* newcol = nullptr, unsigned rowmask = 0xffffffffu) {
   constexpr unsigned FULL = 0xffffffffu;
   const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
@@ -102,12 +102,15 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   if (gl < n) {
     double rix, riy, riz;
     v2.get(f + gl, rix, riy, riz);
+    // rows to recompute (the others come from ecache): every row unless the
+    // cached matrix is valid apart from the rows in rowmask
+    const bool row_new = (rowmask >> gl) & 1u;
     if (sho) {
       const double c = s.node_c[sp], ch = s.node_cosh[sp];
       const double ri2 = dot3(rix, riy, riz, rix, riy, riz);
       for (int j = 0; j < n; ++j) {
         double e;
-        if (ecache && jcol >= 0 && j != jcol) {
+        if (ecache && ((jcol >= 0 && j != jcol) || (jcol < 0 && !row_new))) {
           e = ecache[j * n + gl];
         } else {
           double rjx, rjy, rjz;
@@ -129,7 +132,7 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
       const int nn = n * n;
       for (int j = 0; j < n; ++j) {
         double val, gx, gy, gz;
-        if (ecache && jcol >= 0 && j != jcol) {
+        if (ecache && ((jcol >= 0 && j != jcol) || (jcol < 0 && !row_new))) {
           val = ecache[j * n + gl];
           gx = ecache[nn + j * n + gl];
           gy = ecache[2 * nn + j * n + gl];
