@@ -101,13 +101,16 @@ def sweep_attempts(kw):
 # ------------------------------------------------------- measured work per unit
 # Thread-level FP64 flops (DADD + DMUL + 2 DFMA, predicated-on lanes only) and
 # DRAM bytes (read + write) per section attempt of the section kernel, counted
-# by ncu on the same kernel and workload in the steady state (the timed sweep of
-# a 304-replica run after a warm-up sweep).  The commands and raw counts are in
+# by ncu on the same kernel and workload after a warm-up step (the timed step of
+# a bench run).  The commands and raw counts are in
 # profiles/fp64_work_per_attempt.md; they are the roofline numerator.
 MEASURED_WORK = {
     # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
-    ("dot20_fn", "mixed"): (299983.4, None),
-    ("dot20_fn", "fp64"): (518953.4, None),
+    ("dot20_fn", "mixed"): (2.654e5, 8.201e4),
+    ("dot20_fn", "fp64"): (4.872e5, 8.206e4),
+    ("batch4096", "mixed"): (2.334e5, 3.26e4),   # counted on the first 1024 replicas
+    ("heg54", "mixed"): (1.097e7, 1.499e6),
+    ("dot2", "fp64"): (1.933e4, 459.6),
 }
 
 
@@ -348,6 +351,8 @@ def run_engine(args, rank, world):
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
     kws = workload_kw(args.workload)
     batch = isinstance(kws, list)
+    if batch and args.replicas:
+        kws = kws[:args.replicas]  # the first replicas of the mix (smaller profiling runs)
     R0, A0 = defaults(args.workload)
     R = len(kws) if batch else (args.replicas or R0)
     kw = kws[0] if batch else kws
