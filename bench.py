@@ -153,6 +153,23 @@ def attempt_flops(kw, reach):
     return total
 
 
+# ----------------------------------------------------------- ranks (torchrun)
+def max_over_ranks(x, world, device="cuda"):
+    """The largest x over the ranks (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed(rank):
+    """Each rank runs its own replicas: distinct random streams per rank."""
+    return 20261203 + 1000003 * rank
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     def __init__(self):
@@ -279,7 +296,7 @@ def run_serve(args, rank, world):
     kw0 = WL.serve_stream(1)[0][1]
     base, _ = pimc_gb300.coulomb_tables(dict(kw0, counts=[2, 2], node_kind=[1, 1],
                                              node_omega=[1.0, 1.0], sho_omega=[1.0, 1.0]))
-    seed = 20261203 + 1000003 * rank
+    seed = rank_seed(rank)
     pool = int(args.pool_gb * (1 << 30))
     srv = pimc_gb300.Server(args.slots, pool, 64, 2048, 5, 32, seed=seed, precision=prec)
     stream = torch.cuda.current_stream()
@@ -299,10 +316,7 @@ def run_serve(args, rank, world):
         loop.run(reqs, realtime=True)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([wall], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        wall = float(t.item())
+    wall = max_over_ranks(wall, world)
     summ = serving.summary(reqs, wall)
     beads = summ["bead_updates"]
     offered = sum(r.beads for r in reqs) / max(reqs[-1].arrival, 1e-9)
@@ -358,7 +372,7 @@ def run_engine(args, rank, world):
     kw = kws[0] if batch else kws
     A = args.attempts or A0 or sweep_attempts(kw)
     prec = pimc_gb300.PIMC_PREC_MIXED if args.precision == "mixed" else pimc_gb300.PIMC_PREC_FP64
-    seed = 20261203 + 1000003 * rank
+    seed = rank_seed(rank)
     if batch:
         base, _ = pimc_gb300.coulomb_tables(dict(kw, counts=[2, 2], node_kind=[1, 1],
                                                  node_omega=[1.0, 1.0], sho_omega=[1.0, 1.0]))
@@ -413,10 +427,7 @@ def run_engine(args, rank, world):
     energy = eng.thermo_energy()  # energies after the last step (untimed re-measurement)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+    t_ms = max_over_ranks(t_ms, world)
     units = A * sum((1 << k["nlevel"]) - 1 for k in systems)
     value = world * units * args.steps / (t_ms * 1e-3)
     # ---- end to end through the public API, host buffers each step
