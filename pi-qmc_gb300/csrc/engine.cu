@@ -15,6 +15,7 @@
 #include "kernels.cuh"
 #include "noalloc_kernel.cuh"
 #include "displace_kernel.cuh"
+#include "prefill_kernel.cuh"
 
 namespace pimc {
 // register-budget variants of the section kernel (section_variants.cu)
@@ -126,6 +127,8 @@ struct pimc_engine {
   size_t table_used = 0;
   DevBuf<double> d_pool;
   DevBuf<int> d_slot_attempts;  // attempts per round of each slot
+  std::vector<int> prefill_pending;  // admitted slots whose Slater cache is still empty
+  DevBuf<int> d_prefill;
   std::vector<int> slot_attempts;
   bool order_dirty = true;
   int nactive = 0;
@@ -160,6 +163,7 @@ struct pimc_engine {
     d_next.free();
     d_pool.free();
     d_slot_attempts.free();
+    d_prefill.free();
     d_ugrid.free();
     d_ugrid32.free();
     d_kvec.free();
@@ -686,12 +690,56 @@ int pimc_set_stream(pimc_engine* e, void* stream) {
   return PIMC_OK;
 }
 
+namespace {
+// Fills the Slater-result cache entries of `nslot` replicas (slots on the device,
+// or null for 0 .. nslot-1) from their current paths, one warp per entry.
+int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) {
+  int nsp = 0, mmax = 0, nmax = 0;
+  bool anyfree = false, any = false;
+  for (int r = 0; r < e->nrep; ++r) {
+    const DevSys& d = e->hsys[r];
+    if (!(d.fixed_node && d.nc_offset >= 0)) continue;
+    any = true;
+    nsp = std::max(nsp, d.nspecies);
+    mmax = std::max(mmax, d.nslice);
+    for (int i = 0; i < d.nspecies; ++i)
+      if (d.node_kind[i]) {
+        nmax = std::max(nmax, d.spec_count[i]);
+        anyfree |= d.node_kind[i] == PIMC_NODES_FREE;
+      }
+  }
+  if (!any || nslot == 0) return PIMC_OK;
+  PrefillParams P;
+  P.sys = e->d_sys.p;
+  P.state = e->d_state.p;
+  P.paths = e->server ? e->d_pool.p : e->d_paths.p;
+  P.cache = cache;
+  P.slots = d_slots;
+  P.nslot = nslot;
+  P.ntask_per_slot = nsp * mmax;
+  P.stage_stride = (6 * nmax + 1) & ~1;
+  P.scratch_stride = (node_group_scratch(nmax, anyfree) + 1) & ~1;
+  const size_t per_warp = (size_t)(P.stage_stride + P.scratch_stride) * 8;
+  const int nw = (int)std::max<size_t>(1, std::min<size_t>(kBlock / 32, (200 * 1024) / per_warp));
+  cudaFuncSetAttribute(cache_prefill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
+  const dim3 grid((P.ntask_per_slot + nw - 1) / nw, nslot);
+  cache_prefill_kernel<<<grid, 32 * nw, per_warp * nw, e->stream>>>(P);
+  e->launches++;
+  CU(cudaGetLastError());
+  return PIMC_OK;
+}
+}  // namespace
+
 int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (!e || !host_xyz) return fail(PIMC_ERR_INVALID, "null argument");
+  if (e->server) return fail(PIMC_ERR_INVALID, "a server takes paths at admission");
   CU(cudaMemcpyAsync(e->d_paths.p, host_xyz, e->path_off[e->nrep] * sizeof(double),
                      cudaMemcpyHostToDevice, e->stream));
-  if (e->d_nodecache.p)  // new paths: every cached Slater result is stale
+  if (e->d_nodecache.p) {  // new paths: every cached Slater result is rebuilt
     CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double), e->stream));
+    if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep)) return rc;
+  }
   return PIMC_OK;
 }
 
@@ -1504,6 +1552,7 @@ int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_ta
                      e->stream));
   CU(cudaMemcpyAsync(e->d_state.p + r, &st, sizeof(DevState), cudaMemcpyHostToDevice, e->stream));
   e->slot_attempts[r] = round_attempts;
+  if (cw) e->prefill_pending.push_back(r);
   CU(cudaMemcpyAsync(e->d_slot_attempts.p + r, &e->slot_attempts[r], sizeof(int),
                      cudaMemcpyHostToDevice, e->stream));
   CU(cudaMemcpyAsync(e->d_pool.p + po, host_path, pw * sizeof(double), cudaMemcpyHostToDevice,
@@ -1528,6 +1577,21 @@ int pimc_server_run(pimc_engine* e) {
   if (!e || !e->server) return fail(PIMC_ERR_INVALID, "bad argument");
   if (int rc = refresh_order(e)) return rc;
   if (e->nactive == 0) return PIMC_OK;
+  if (!e->prefill_pending.empty()) {
+    // newly admitted simulations: their Slater caches, filled in parallel
+    std::vector<int> live;
+    for (int r : e->prefill_pending)
+      if (e->active[r]) live.push_back(r);
+    e->prefill_pending.clear();
+    if (!live.empty()) {
+      if (e->d_prefill.n < live.size() && e->d_prefill.alloc(std::max<size_t>(live.size(), 64)))
+        return fail(PIMC_ERR_CUDA, "cudaMalloc prefill list");
+      CU(cudaMemcpyAsync(e->d_prefill.p, live.data(), live.size() * sizeof(int),
+                         cudaMemcpyHostToDevice, e->stream));
+      if (int rc = prefill_cache(e, e->d_pool.p, e->d_prefill.p, (int)live.size())) return rc;
+      CU(cudaStreamSynchronize(e->stream));  // the host list is reused next round
+    }
+  }
   const int nattempt = 0;
   RunParams P;
   P.sys = e->d_sys.p;
