@@ -155,6 +155,43 @@ int pimc_download_paths(pimc_engine* e, double* host_xyz);
  * engines of one system this is r * nslice * npart * 3. */
 int pimc_path_offsets(pimc_engine* e, int64_t* offsets /* nreplica+1 */);
 
+/* ---- checkpoints (WritePaths / PathReader, and the random-stream position) */
+
+/* Path files in pi-qmc's restart format: "#Permutations ..." (the identity),
+ * "#Path coordinates: N particles in 3-d", then one line per slice with every
+ * particle's x y z at 15 significant digits, each followed by a space
+ * (WritePaths::run, src/algorithm/WritePaths.cc:25-114).  xyz is one
+ * replica's host path, [nslice][npart][3]. */
+int pimc_paths_write_file(const char* filename, const double* xyz, int npart, int nslice);
+/* Reads such a file as PathReader::run does (src/algorithm/PathReader.cc:20-140):
+ * the "#Permutations" line is optional (without it a last, wrapped slice is
+ * read and matched to the first), file slice k fills slices
+ * k + ib*nslice/bfactor for ib < bfactor.  Files whose permutation is not the
+ * identity, that end early or that hold a non-number are rejected
+ * (PIMC_ERR_INVALID); xyz is left unchanged then. */
+int pimc_paths_read_file(const char* filename, double* xyz, int npart, int nslice, int bfactor);
+/* The same for replica `replica` of an engine (an active slot of a server for
+ * writing).  Reading replaces that replica's path only and rebuilds its cached
+ * Slater results; servers take paths at admission instead. */
+int pimc_write_paths(pimc_engine* e, int replica, const char* filename);
+int pimc_read_paths(pimc_engine* e, int replica, const char* filename, int bfactor);
+
+/* Everything besides the path that decides a replica's future moves: the
+ * position of its random stream (attempts made), its acceptance counts and
+ * status word, and the node models' determinant scales (SHONodes /
+ * FreeParticleNodes rescale the matrix to keep det in range).  A replica whose
+ * path (exact doubles: pimc_download_paths / pimc_upload_paths) and state are
+ * copied into another engine of the same system and seed continues the
+ * identical chain. */
+typedef struct {
+  uint32_t attempt;   /* section/displace attempts drawn from the replica's stream */
+  uint32_t status;    /* PIMC_STATUS_* bits */
+  int64_t accepted, attempted;
+  double node_scale[PIMC_MAX_SPECIES];
+} pimc_replica_state;
+int pimc_get_replica_state(pimc_engine* e, int replica, pimc_replica_state* out);
+int pimc_set_replica_state(pimc_engine* e, int replica, const pimc_replica_state* in);
+
 /* ---- the sampler ------------------------------------------------------- */
 
 /* Runs nattempt section-move attempts on every replica, on the device, in
@@ -217,6 +254,22 @@ int pimc_ewald_coulomb_energy(pimc_engine* e, double epsilon, double rcut,
 /* Builds that Ewald table and grid for a system (host only, no GPU). */
 int pimc_ewald_estimator_tables(const pimc_system* sys, double rcut, double kcut, double epsilon,
                                 const pimc_ewald_table** est, double* vgrid);
+
+/* ---- host-built action tables (no GPU) ----------------------------------- */
+
+/* The tables CoulombAction's constructor builds (src/action/CoulombAction.cc:19-91
+ * with PairAction's empirical-action grid, src/action/PairAction.cc:161-185):
+ * one pair table per interacting species pair i <= j, and with sys->ewald the
+ * OptEwaldSum long-range table (src/util/OptEwaldSum.cc:28-245) for real-space
+ * cutoff ewald_rcut (0: half the first box side) and k cutoff ewald_kcut.
+ * ngpts 0 / rmin 0 / rmax 0 take pi-qmc's defaults.  The arrays stay valid
+ * until the next call on the same thread; *ewald is NULL without Ewald. */
+int pimc_coulomb_tables(const pimc_system* sys, int norder, int ngpts, double rmin, double rmax,
+                        double ewald_rcut, double ewald_kcut, const pimc_pair_table** tables,
+                        int* ntables, const pimc_ewald_table** ewald);
+/* The short-range polynomial coefficients (n of them) of the last Ewald table
+ * pimc_coulomb_tables built on this thread. */
+int pimc_ewald_coefficients(double* coef, int n);
 
 /* ---- launch configuration and autotuning -------------------------------- */
 

@@ -40,6 +40,7 @@ SOURCES = [
     "estimator/EwaldCoulombEstimator.cc", "stats/ScalarEstimator.cc",
     "stats/SimpleScalarAccumulator.cpp", "advancer/DisplaceMoveSampler.cc",
     "advancer/DoubleDisplaceMoveSampler.cc", "advancer/UniformMover.cc",
+    "algorithm/WritePaths.cc", "algorithm/PathReader.cc",
 ]
 
 FLAGS = ["-std=gnu++98", "-O2", "-fPIC", "-w", "-ffp-contract=off", "-DHAVE_CONFIG_H"]

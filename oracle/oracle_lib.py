@@ -243,6 +243,8 @@ class RefOracle(_Base):
             L.ref_coulomb_u.argtypes = [C.c_void_p, C.c_double, C.c_int]
             L.ref_coulomb_utau.restype = C.c_double
             L.ref_coulomb_utau.argtypes = [C.c_void_p, C.c_double, C.c_int]
+            L.ref_write_paths.argtypes = [C.c_void_p, C.c_char_p]
+            L.ref_read_paths.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
             cls._lib = L
         return cls._lib
 
@@ -284,6 +286,14 @@ class RefOracle(_Base):
 
     def thermo_energy(self):
         return self.lib().ref_thermo_energy(self.h)
+
+    def write_paths(self, filename):
+        """WritePaths::run on the current path (pi-qmc's restart file)."""
+        self.lib().ref_write_paths(self.h, os.fsencode(filename))
+
+    def read_paths(self, filename, bfactor=1):
+        """PathReader::run into the current path."""
+        self.lib().ref_read_paths(self.h, os.fsencode(filename), bfactor)
 
     def action_diff(self, level, section, moving, ipart):
         section = np.ascontiguousarray(section, np.float64)

@@ -53,6 +53,8 @@
 #include "util/EwaldSum.h"
 #include "util/OptEwaldSum.h"
 #include "util/SuperCell.h"
+#include "algorithm/PathReader.h"
+#include "algorithm/WritePaths.h"
 #undef private
 #undef protected
 
@@ -373,6 +375,23 @@ extern "C" void ref_get_path(void* h, double* xyz) {
   for (int t = 0; t < ns; ++t)
     for (int i = 0; i < np; ++i)
       for (int d = 0; d < 3; ++d) xyz[(t * np + i) * 3 + d] = (*s->paths)(i, t)[d];
+}
+
+// WritePaths::run (src/algorithm/WritePaths.cc:25-114) on the current path:
+// dumpFreq 0 writes on the first call; no movie file.
+extern "C" void ref_write_paths(void* h, const char* filename) {
+  RefSim* s = (RefSim*)h;
+  WritePaths w(*s->paths, std::string(filename), 0, 1, false, *s->simInfo, 0,
+               s->simInfo->getBeadFactory());
+  w.run();
+}
+
+// PathReader::run (src/algorithm/PathReader.cc:20-140) into the current path.
+extern "C" void ref_read_paths(void* h, const char* filename, int bfactor) {
+  RefSim* s = (RefSim*)h;
+  std::string name(filename);
+  PathReader r(*s->paths, name, s->simInfo->getBeadFactory(), bfactor, 0);
+  r.run();
 }
 
 // Runs n section-move attempts numbered first_attempt, first_attempt+1, ...

@@ -62,6 +62,15 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace
+
+namespace pimc {
+// Error reporting for the host-only files of the library (paths_io.cc).
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace pimc
+
+namespace {
+
 #define CU(call)                                                                      \
   do {                                                                                \
     cudaError_t e_ = (call);                                                          \
@@ -754,6 +763,107 @@ int pimc_download_paths(pimc_engine* e, double* host_xyz) {
 int pimc_path_offsets(pimc_engine* e, int64_t* offsets) {
   if (!e || !offsets) return fail(PIMC_ERR_INVALID, "null argument");
   for (int r = 0; r <= e->nrep; ++r) offsets[r] = e->path_off[r];
+  return PIMC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Device address and shape of replica r's path (an active slot on a server).
+int replica_path(pimc_engine* e, int r, double** dev, int* npart, int* nslice) {
+  if (!e || r < 0 || r >= e->nrep) return fail(PIMC_ERR_INVALID, "bad replica");
+  if (e->server && !e->active[r]) return fail(PIMC_ERR_INVALID, "slot not in use");
+  const DevSys& d = e->hsys[r];
+  *dev = (e->server ? e->d_pool.p : e->d_paths.p) + d.path_offset;
+  *npart = d.npart;
+  *nslice = d.nslice;
+  return PIMC_OK;
+}
+
+// Rebuilds replica r's Slater-result cache from its current path and state.
+int refresh_cache(pimc_engine* e, int r) {
+  const DevSys& d = e->hsys[r];
+  if (!(d.fixed_node && d.nc_offset >= 0)) return PIMC_OK;
+  double* base = e->server ? e->d_pool.p : e->d_nodecache.p;
+  CU(cudaMemsetAsync(base + d.nc_offset, 0xff,
+                     (size_t)d.nspecies * d.nslice * d.nc_stride * sizeof(double), e->stream));
+  if (e->d_prefill.n < 1 && e->d_prefill.alloc(64))
+    return fail(PIMC_ERR_CUDA, "cudaMalloc prefill list");
+  CU(cudaMemcpyAsync(e->d_prefill.p, &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  return prefill_cache(e, base, e->d_prefill.p, 1);
+}
+}  // namespace
+
+extern "C" {
+
+int pimc_write_paths(pimc_engine* e, int replica, const char* filename) {
+  double* dev;
+  int npart, nslice;
+  if (int rc = replica_path(e, replica, &dev, &npart, &nslice)) return rc;
+  std::vector<double> h((size_t)npart * nslice * 3);
+  CU(cudaMemcpyAsync(h.data(), dev, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                     e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return pimc_paths_write_file(filename, h.data(), npart, nslice);
+}
+
+int pimc_read_paths(pimc_engine* e, int replica, const char* filename, int bfactor) {
+  double* dev;
+  int npart, nslice;
+  if (int rc = replica_path(e, replica, &dev, &npart, &nslice)) return rc;
+  if (e->server) return fail(PIMC_ERR_INVALID, "a server takes paths at admission");
+  std::vector<double> h((size_t)npart * nslice * 3);
+  if (int rc = pimc_paths_read_file(filename, h.data(), npart, nslice, bfactor)) return rc;
+  CU(cudaMemcpyAsync(dev, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                     e->stream));
+  if (int rc = refresh_cache(e, replica)) return rc;
+  CU(cudaStreamSynchronize(e->stream));  // h goes out of scope
+  return PIMC_OK;
+}
+
+int pimc_get_replica_state(pimc_engine* e, int replica, pimc_replica_state* out) {
+  double* dev;
+  int npart, nslice;
+  if (int rc = replica_path(e, replica, &dev, &npart, &nslice)) return rc;
+  if (!out) return fail(PIMC_ERR_INVALID, "null argument");
+  DevState st;
+  CU(cudaMemcpyAsync(&st, e->d_state.p + replica, sizeof(DevState), cudaMemcpyDeviceToHost,
+                     e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  memset(out, 0, sizeof(*out));
+  out->attempt = st.attempt;
+  out->status = st.status;
+  out->accepted = st.accepted;
+  out->attempted = st.attempted;
+  for (int k = 0; k < PIMC_MAX_SPECIES; ++k) out->node_scale[k] = st.node_scale[k];
+  return PIMC_OK;
+}
+
+int pimc_set_replica_state(pimc_engine* e, int replica, const pimc_replica_state* in) {
+  double* dev;
+  int npart, nslice;
+  if (int rc = replica_path(e, replica, &dev, &npart, &nslice)) return rc;
+  if (!in) return fail(PIMC_ERR_INVALID, "null argument");
+  for (int k = 0; k < PIMC_MAX_SPECIES; ++k)
+    if (!(in->node_scale[k] > 0) || !std::isfinite(in->node_scale[k]))
+      return fail(PIMC_ERR_INVALID, "node scales must be positive and finite");
+  DevState st;
+  CU(cudaMemcpyAsync(&st, e->d_state.p + replica, sizeof(DevState), cudaMemcpyDeviceToHost,
+                     e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  st.attempt = in->attempt;
+  st.status = in->status;
+  st.accepted = in->accepted;
+  st.attempted = in->attempted;
+  for (int k = 0; k < kMaxSpecies; ++k) {
+    if (st.node_scale[k] != in->node_scale[k]) st.epoch[k]++;
+    st.node_scale[k] = in->node_scale[k];
+  }
+  CU(cudaMemcpyAsync(e->d_state.p + replica, &st, sizeof(DevState), cudaMemcpyHostToDevice,
+                     e->stream));
+  // cached Slater results were made at the old scales
+  if (int rc = refresh_cache(e, replica)) return rc;
+  CU(cudaStreamSynchronize(e->stream));
   return PIMC_OK;
 }
 

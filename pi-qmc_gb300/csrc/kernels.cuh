@@ -283,7 +283,7 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
   for (int sp = 0; sp < s.nspecies; ++sp) {
     if (!s.node_kind[sp]) continue;
     const int n = s.spec_count[sp];
-    const int W = node_group_width(n), G = 32 / W, g = lane / W, gl = lane & (W - 1);
+    const int W = node_group_width(n), g = lane / W;
     const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
     double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
     const bool mine = sp == msp;

@@ -19,7 +19,7 @@ MAXL = 6
 PIMC_NODES_NONE, PIMC_NODES_SHO, PIMC_NODES_FREE = 0, 1, 2
 PIMC_MOVER_FREE, PIMC_MOVER_FREE_PBC = 0, 1
 PIMC_PREC_FP64, PIMC_PREC_MIXED = 0, 1
-PIMC_ERR_CAPACITY = -4
+PIMC_ERR_INVALID, PIMC_ERR_CUDA, PIMC_ERR_NO_DEVICE, PIMC_ERR_CAPACITY = -1, -2, -3, -4
 STATUS_BITS = {1: "init_crossing", 2: "singular", 4: "rescale_limit", 8: "nonfinite"}
 
 
@@ -70,6 +70,24 @@ class DisplaceRecord(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int), ("hbm_bytes", C.c_size_t), ("max_npart", C.c_int),
                 ("max_nslice", C.c_int), ("max_level", C.c_int), ("max_node_count", C.c_int)]
+
+
+class ReplicaState(C.Structure):
+    _fields_ = [("attempt", C.c_uint32), ("status", C.c_uint32), ("accepted", C.c_int64),
+                ("attempted", C.c_int64), ("node_scale", C.c_double * 4)]
+
+    def as_dict(self):
+        return {"attempt": self.attempt, "status": self.status, "accepted": self.accepted,
+                "attempted": self.attempted, "node_scale": list(self.node_scale)}
+
+    @classmethod
+    def from_dict(cls, d):
+        st = cls()
+        st.attempt, st.status = d["attempt"], d["status"]
+        st.accepted, st.attempted = d["accepted"], d["attempted"]
+        for k, v in enumerate(d["node_scale"]):
+            st.node_scale[k] = v
+        return st
 
 
 class MoveRecord(C.Structure):
@@ -166,6 +184,12 @@ def lib():
         L.pimc_server_pool.argtypes = [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.pimc_kernel_launches.argtypes = [P]
         L.pimc_kernel_launches.restype = C.c_int64
+        L.pimc_paths_write_file.argtypes = [C.c_char_p, D, I, I]
+        L.pimc_paths_read_file.argtypes = [C.c_char_p, D, I, I, I]
+        L.pimc_write_paths.argtypes = [P, I, C.c_char_p]
+        L.pimc_read_paths.argtypes = [P, I, C.c_char_p, I]
+        L.pimc_get_replica_state.argtypes = [P, I, C.POINTER(ReplicaState)]
+        L.pimc_set_replica_state.argtypes = [P, I, C.POINTER(ReplicaState)]
         _lib = L
     return _lib
 
@@ -177,6 +201,36 @@ def _check(rc):
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def write_paths_file(filename, xyz):
+    """One path [nslice][npart][3] to a file in pi-qmc's restart format
+    (WritePaths, src/algorithm/WritePaths.cc:25-114)."""
+    x = np.ascontiguousarray(xyz, np.float64)
+    _check(lib().pimc_paths_write_file(os.fsencode(filename), _dp(x), x.shape[1], x.shape[0]))
+
+
+def read_paths_file(filename, npart, nslice, bfactor=1):
+    """A restart file read as PathReader does (src/algorithm/PathReader.cc:20-140)."""
+    out = np.zeros((nslice, npart, 3))
+    _check(lib().pimc_paths_read_file(os.fsencode(filename), _dp(out), npart, nslice, bfactor))
+    return out
+
+
+class _Checkpoint:
+    """Restart files and random-stream state of one replica (a slot on a server)."""
+
+    def write_paths(self, replica, filename):
+        _check(lib().pimc_write_paths(self.h, replica, os.fsencode(filename)))
+
+    def replica_state(self, replica):
+        st = ReplicaState()
+        _check(lib().pimc_get_replica_state(self.h, replica, C.byref(st)))
+        return st.as_dict()
+
+    def set_replica_state(self, replica, state):
+        st = ReplicaState.from_dict(state)
+        _check(lib().pimc_set_replica_state(self.h, replica, C.byref(st)))
 
 
 def pair_tables_struct(tables):
@@ -240,7 +294,7 @@ def stream_sample(seed, replica, attempt, n):
     return u, z
 
 
-class Engine:
+class Engine(_Checkpoint):
     """A set of replicas advanced on the GPU (pimc_engine).
 
     ``Engine(system_kw, nreplica, tables, ewald, seed)`` builds replicas of one
@@ -323,6 +377,10 @@ class Engine:
             return out
         return [out[self.offsets[r]:self.offsets[r + 1]].reshape(self.path_shape(r))
                 for r in range(self.nreplica)]
+
+    def read_paths(self, replica, filename, bfactor=1):
+        """Replaces one replica's path with a restart file's."""
+        _check(lib().pimc_read_paths(self.h, replica, os.fsencode(filename), bfactor))
 
     # sampler --------------------------------------------------------------
     def run_sections(self, nattempt, records=False):
@@ -456,7 +514,7 @@ class Engine:
         return lib().pimc_kernel_launches(self.h)
 
 
-class Server:
+class Server(_Checkpoint):
     """Slots of independent simulations over one device pool (pimc_server_*).
 
     ``admit`` places a simulation in a free slot when its path and Slater-result

@@ -13,7 +13,7 @@ CSRC = os.path.join(ROOT, "csrc")
 LIB = os.path.join(PKG, "libpimc_gb300.so")
 # (source, extra flags): the section kernel's register-budget variants are
 # separate objects so that nvcc compiles them in parallel
-SOURCES = [("engine.cu", []), ("tables.cc", [])] + [
+SOURCES = [("engine.cu", []), ("tables.cc", []), ("paths_io.cc", [])] + [
     ("section_variants.cu", [f"-DPIMC_NT={nt}", f"-DPIMC_MINB={v}"])
     for nt, v in ((256, 2), (256, 3), (256, 4), (512, 1))]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

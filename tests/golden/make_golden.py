@@ -10,7 +10,9 @@ and, on the final path, the thermodynamic, virial (windows 1, 4, 16) and
 Coulomb energy estimators (direct, and for periodic cases the optimized-Ewald
 estimator together with the Ewald table and short-range grid it built), and
 for some cases a recorded run of rigid-displacement moves from the final path
-(DisplaceMoveSampler / DoubleDisplaceMoveSampler with a UniformMover).
+(DisplaceMoveSampler / DoubleDisplaceMoveSampler with a UniformMover).  For two
+cases the final path is also written by pi-qmc's WritePaths (<case>.paths) and
+read back by its PathReader (path_files.npz).
 
 The fixtures let machines without the reference tree (the GPU machine) pin the C++
 restatement and the CUDA engine against the reference's own outputs.
@@ -101,9 +103,48 @@ def run_case(name, kw, init, nattempt):
           f"E={e1:.6f}, {os.path.getsize(path) / 1024:.0f} KiB")
 
 
+# restart files: pi-qmc's WritePaths on the final path of these cases, and what
+# its PathReader makes of that file and of two variants (no permutation line
+# with a wrapped last slice; half the slices, read with bfactor 2)
+PATH_FILES = ("dot2_small", "dot4_fn")
+
+
+def make_path_files():
+    out = {}
+    for name in PATH_FILES:
+        kw, init, n = W.GOLDEN_CASES[name]
+        z = np.load(os.path.join(HERE, name + ".npz"))
+        x1 = z["path0"] + z["dpath"]
+        ref = O.RefOracle(O.make_config(**kw))
+        ref.set_path(x1)
+        fname = os.path.join(HERE, name + ".paths")
+        ref.write_paths(fname)
+        lines = open(fname).read().splitlines(keepends=True)
+        variants = {name: (fname, 1)}
+        if name == "dot4_fn":
+            m = kw["nslice"]
+            noperm = os.path.join(HERE, name + "_noperm.paths")
+            with open(noperm, "w") as f:
+                f.writelines(lines[1:] + [lines[2]])
+            half = os.path.join(HERE, name + "_half.paths")
+            with open(half, "w") as f:
+                f.writelines(lines[:2 + m // 2])
+            variants[name + "_noperm"] = (noperm, 1)
+            variants[name + "_half"] = (half, 2)
+        for key, (fn, bfactor) in variants.items():
+            ref.set_path(np.zeros_like(x1))
+            ref.read_paths(fn, bfactor)
+            out[key + "_read"] = ref.get_path()
+            out[key + "_bfactor"] = np.array(bfactor)
+        out[name + "_path"] = x1
+    np.savez_compressed(os.path.join(HERE, "path_files.npz"), **out)
+    print("path files:", ", ".join(k[:-5] for k in out if k.endswith("_read")))
+
+
 def main():
     for name, (kw, init, n) in W.GOLDEN_CASES.items():
         run_case(name, kw, init, n)
+    make_path_files()
 
 
 if __name__ == "__main__":
