@@ -119,6 +119,9 @@ struct pimc_engine {
   DevBuf<double> d_paths;
   DevBuf<double> d_nodescr;
   DevBuf<double> d_nodecache;
+  DevBuf<long long> d_ekcache;  // structure factors per replica and slice
+  DevBuf<long long> d_ekstage;  // per-CTA staging of an attempt's new structure factors
+  int ekstage_stride = 0;       // int64 words per CTA
   DevBuf<int> d_order;
   DevBuf<int> d_next;
   DevBuf<double> d_ugrid;
@@ -168,6 +171,8 @@ struct pimc_engine {
     d_paths.free();
     d_nodescr.free();
     d_nodecache.free();
+    d_ekcache.free();
+    d_ekstage.free();
     d_order.free();
     d_next.free();
     d_pool.free();
@@ -229,6 +234,8 @@ int validate(const pimc_system& s) {
 
 void fill_sys(const pimc_system& s, DevSys& d) {
   memset(&d, 0, sizeof(d));
+  d.ek_offset = -1;
+  d.ek_scale = 1.0;
   d.npart = s.npart;
   d.nspecies = s.nspecies;
   d.nslice = s.nslice;
@@ -446,6 +453,8 @@ int device_check(int& nsm) {
   return 0;
 }
 
+int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot);
+
 int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables,
                  const int* tab_off, int uniform, const pimc_ewald_table* ewald, uint64_t seed,
                  int precision, pimc_engine** out) {
@@ -626,6 +635,31 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
       cudaMemset(e->d_nodecache.p, 0xff, coff * sizeof(double));  // NaN epochs: all invalid
     }
   }
+  // Structure-factor cache of Ewald systems (left out, like the Slater cache,
+  // when an attempt's two sections can overlap, and when the charges are too
+  // large for a fine fixed-point grid).
+  {
+    long long eoff = 0;
+    for (DevSys& d : e->hsys) {
+      d.ek_offset = -1;
+      if (!(d.ewald && d.coulomb && d.totk > 0)) continue;
+      if (d.fixed_node && !((1 << d.nlevel) < d.nslice / 2)) continue;
+      double qsum = 0;
+      for (int i = 0; i < d.nspecies; ++i) qsum += std::fabs(d.charge[i]) * d.spec_count[i];
+      // |rho_k| <= sum |q|; an update adds at most 2 max|q| more: 60 bits cover 3 sum |q|
+      const int ebits = 60 - (int)std::ceil(std::log2(std::max(qsum, 1.0)) + 1e-9);
+      if (ebits < 24) continue;
+      d.ek_scale = std::ldexp(1.0, ebits);
+      d.ek_offset = eoff;
+      eoff += 2LL * d.nslice * d.totk;
+      e->ekstage_stride = std::max(e->ekstage_stride, 2 * (d.nsec - 2) * d.totk);
+    }
+    if (eoff > 0 && (e->d_ekcache.alloc(eoff) ||
+                     e->d_ekstage.alloc((size_t)e->grid * e->ekstage_stride))) {
+      delete e;
+      return fail(PIMC_ERR_CUDA, "cudaMalloc structure-factor cache");
+    }
+  }
   if (e->d_sys.alloc(nrep) || e->d_state.alloc(nrep) || e->d_paths.alloc(off)) {
     delete e;
     return fail(PIMC_ERR_CUDA, "cudaMalloc engine state");
@@ -660,6 +694,10 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   }
   cudaMemcpy(e->d_state.p, st.data(), nrep * sizeof(DevState), cudaMemcpyHostToDevice);
   cudaMemset(e->d_paths.p, 0, off * sizeof(double));
+  if (int rc = prefill_ewald(e, nullptr, nrep)) {  // structure factors of the zero paths
+    delete e;
+    return rc;
+  }
   CU(cudaDeviceSynchronize());
   *out = e;
   return PIMC_OK;
@@ -698,6 +736,8 @@ int pimc_set_stream(pimc_engine* e, void* stream) {
   e->stream = (cudaStream_t)stream;
   return PIMC_OK;
 }
+
+}  // extern "C"
 
 namespace {
 // Fills the Slater-result cache entries of `nslot` replicas (slots on the device,
@@ -738,7 +778,38 @@ int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) 
   CU(cudaGetLastError());
   return PIMC_OK;
 }
+
+// Fills the structure-factor cache of `nslot` replicas (device slot list, or
+// null for 0 .. nslot-1) from their current paths.
+int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot) {
+  if (!e->d_ekcache.p || nslot == 0) return PIMC_OK;
+  int mmax = 0, np = 0, per = 0;
+  for (const DevSys& d : e->hsys) {
+    if (d.ek_offset < 0) continue;
+    mmax = std::max(mmax, d.nslice);
+    np = std::max(np, d.npart);
+    per = std::max(per, d.ikmax[0] + 1 + 2 * d.ikmax[1] + 1 + 2 * d.ikmax[2] + 1);
+  }
+  if (mmax == 0) return PIMC_OK;
+  EkPrefillParams P;
+  P.sys = e->d_sys.p;
+  P.paths = e->d_paths.p;
+  P.ek = e->d_ekcache.p;
+  P.slots = d_slots;
+  P.nslot = nslot;
+  P.nslice_max = mmax;
+  const size_t smem = (size_t)per * np * 16 + (size_t)np * 8;
+  if (smem > 200 * 1024) return fail(PIMC_ERR_CAPACITY, "Ewald tables exceed shared memory");
+  cudaFuncSetAttribute(ewald_prefill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
+  ewald_prefill_kernel<<<dim3(mmax, nslot), kBlock, smem, e->stream>>>(P);
+  e->launches++;
+  CU(cudaGetLastError());
+  return PIMC_OK;
+}
 }  // namespace
+
+extern "C" {
 
 int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (!e || !host_xyz) return fail(PIMC_ERR_INVALID, "null argument");
@@ -749,7 +820,7 @@ int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
     CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double), e->stream));
     if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep)) return rc;
   }
-  return PIMC_OK;
+  return prefill_ewald(e, nullptr, e->nrep);
 }
 
 int pimc_download_paths(pimc_engine* e, double* host_xyz) {
@@ -783,14 +854,18 @@ int replica_path(pimc_engine* e, int r, double** dev, int* npart, int* nslice) {
 // Rebuilds replica r's Slater-result cache from its current path and state.
 int refresh_cache(pimc_engine* e, int r) {
   const DevSys& d = e->hsys[r];
-  if (!(d.fixed_node && d.nc_offset >= 0)) return PIMC_OK;
-  double* base = e->server ? e->d_pool.p : e->d_nodecache.p;
-  CU(cudaMemsetAsync(base + d.nc_offset, 0xff,
-                     (size_t)d.nspecies * d.nslice * d.nc_stride * sizeof(double), e->stream));
+  const bool slater = d.fixed_node && d.nc_offset >= 0, ewald = !e->server && d.ek_offset >= 0;
+  if (!slater && !ewald) return PIMC_OK;
   if (e->d_prefill.n < 1 && e->d_prefill.alloc(64))
     return fail(PIMC_ERR_CUDA, "cudaMalloc prefill list");
   CU(cudaMemcpyAsync(e->d_prefill.p, &r, sizeof(int), cudaMemcpyHostToDevice, e->stream));
-  return prefill_cache(e, base, e->d_prefill.p, 1);
+  if (slater) {
+    double* base = e->server ? e->d_pool.p : e->d_nodecache.p;
+    CU(cudaMemsetAsync(base + d.nc_offset, 0xff,
+                       (size_t)d.nspecies * d.nslice * d.nc_stride * sizeof(double), e->stream));
+    if (int rc = prefill_cache(e, base, e->d_prefill.p, 1)) return rc;
+  }
+  return ewald ? prefill_ewald(e, e->d_prefill.p, 1) : PIMC_OK;
 }
 }  // namespace
 
@@ -904,6 +979,9 @@ void fill_run_params(pimc_engine* e, RunParams& P, int nattempt, pimc_move_recor
   P.paths = e->d_paths.p;
   P.nodescr_g = e->d_nodescr.p;
   P.nodecache = e->d_nodecache.p;
+  P.ekcache = e->d_ekcache.p;
+  P.ekstage = e->d_ekstage.p;
+  P.ekstage_stride = e->ekstage_stride;
   P.rec = d_rec;
   P.order = e->d_order.p;
   P.next = e->d_next.p;
@@ -1072,6 +1150,8 @@ int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmovi
   displace_kernel<<<e->grid, std::min(e->block, kBlock), smem, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
+  // displaced paths: every slice's structure factors are rebuilt
+  if (int rc = prefill_ewald(e, nullptr, e->nrep)) return rc;
   if (records) {
     CU(cudaMemcpyAsync(records, d_rec, sizeof(pimc_displace_record) * (size_t)e->nrep * nattempt,
                        cudaMemcpyDeviceToHost, e->stream));
@@ -1329,6 +1409,11 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
       if (e->d_nodescr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
     }
   }
+  if (e->ekstage_stride > 0 && (size_t)grid * e->ekstage_stride > e->d_ekstage.n) {
+    CU(cudaStreamSynchronize(e->stream));
+    if (e->d_ekstage.alloc((size_t)grid * e->ekstage_stride))
+      return fail(PIMC_ERR_CUDA, "cudaMalloc structure-factor staging");
+  }
   e->lay = L;
   e->lay_opts = opts;
   e->ctas_cap = ctas_cap;
@@ -1365,9 +1450,11 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   if (!e || e->server || nattempt <= 0 || !best) return fail(PIMC_ERR_INVALID, "bad argument");
   // state the trials advance, kept aside and restored before each trial
   DevBuf<double> paths0, cache0;
+  DevBuf<long long> ek0;
   DevBuf<DevState> state0;
   const size_t np_ = e->path_off[e->nrep];
-  if (paths0.alloc(np_) || state0.alloc(e->nrep) || cache0.alloc(e->d_nodecache.n))
+  if (paths0.alloc(np_) || state0.alloc(e->nrep) || cache0.alloc(e->d_nodecache.n) ||
+      ek0.alloc(e->d_ekcache.n))
     return fail(PIMC_ERR_CUDA, "cudaMalloc autotune backup");
   auto copy = [&](bool save) -> int {
     CU(cudaMemcpyAsync(save ? paths0.p : e->d_paths.p, save ? e->d_paths.p : paths0.p,
@@ -1377,6 +1464,9 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
     if (e->d_nodecache.n)
       CU(cudaMemcpyAsync(save ? cache0.p : e->d_nodecache.p, save ? e->d_nodecache.p : cache0.p,
                          e->d_nodecache.n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+    if (e->d_ekcache.n)
+      CU(cudaMemcpyAsync(save ? ek0.p : e->d_ekcache.p, save ? e->d_ekcache.p : ek0.p,
+                         e->d_ekcache.n * sizeof(long long), cudaMemcpyDeviceToDevice, e->stream));
     return PIMC_OK;
   };
   if (int rc = copy(true)) return rc;
@@ -1709,6 +1799,9 @@ int pimc_server_run(pimc_engine* e) {
   P.paths = e->d_pool.p;
   P.nodescr_g = e->d_nodescr.p;
   P.nodecache = e->d_pool.p;
+  P.ekcache = nullptr;  // servers take no Ewald systems
+  P.ekstage = nullptr;
+  P.ekstage_stride = 0;
   P.rec = nullptr;
   P.order = e->d_order.p;
   P.next = e->d_next.p;

@@ -28,6 +28,9 @@ struct RunParams {
   int* next;         // work-queue head, zeroed before each launch
   int nattempt;
   const int* nattempt_r;  // per-replica attempts (null: nattempt for every replica)
+  long long* ekcache;     // structure-factor cache pool (null: none)
+  long long* ekstage;     // per-CTA staging of an attempt's new structure factors
+  int ekstage_stride;     // int64 words per CTA
   int nrep;
   uint64_t seed;
   Layout lay;
@@ -77,6 +80,58 @@ __device__ __forceinline__ int species_of(const DevSys& s, int p) {
 // the identity permutation (SerialPaths::getBeads, src/base/SerialPaths.cc:119-136).
 __device__ __forceinline__ int wrap_slice(int islice, int M) {
   return islice < 0 ? islice + M : (islice < M ? islice : islice - M);
+}
+
+// The level-0 Ewald term of CoulombAction::getActionDifference
+// (src/action/CoulombAction.cc:107-119: evalLongRange of the new minus the old
+// configuration on section slices 1 .. 2^L-1, times tau/epsilon) from the
+// slices' cached structure factors: only the moving particle's term changes,
+// rho'_k = rho_k + q (e^{ik.r'} - e^{ik.r}), exact on the fixed-point grid, and
+// evalLongRange's difference is sum_k 2 v_k (|rho'_k|^2 - |rho_k|^2) / (2V)
+// (the self energy cancels).  O(totk) per slice instead of O(totk N) for each
+// of the two configurations.  rho'_k goes to `stage` for the accept step.
+static __device__ __noinline__ double ewald_level0_cached(const DevSys& s, const Smem& m, int ipart,
+                                             int ifirst1, const long long* ek, long long* stage) {
+  const int np = s.npart, nsec = s.nsec, M = s.nslice, totk = s.totk;
+  const int ky0 = s.ikmax[1], kz0 = s.ikmax[2];
+  const int nx = s.ikmax[0] + 1, ny = 2 * ky0 + 1;
+  const int w = np + 1;      // the tables area holds w bead columns
+  const int chunk = w / 2;   // slices per pass: the old and the new bead of each
+  double2* X = (double2*)m.ewt;
+  double2* Y = X + nx * w;
+  double2* Z = Y + ny * w;
+  const double q = m.qpart[ipart], is = 1.0 / s.ek_scale;
+  double acc = 0.0;
+  for (int t0 = 1; t0 < nsec - 1; t0 += chunk) {
+    const int nt = min(chunk, nsec - 1 - t0);
+    __syncthreads();
+    for (int c = threadIdx.x; c < 2 * nt; c += blockDim.x) {
+      const int t = t0 + (c >> 1);
+      if (c & 1)
+        ewald_bead_tables(s, X, Y, Z, w, c, m.mx[t], m.my[t], m.mz[t]);
+      else
+        ewald_bead_tables(s, X, Y, Z, w, c, m.s1x[t * np + ipart], m.s1y[t * np + ipart],
+                          m.s1z[t * np + ipart]);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nt * totk; it += blockDim.x) {
+      const int tt = it / totk, k = it - tt * totk, t = t0 + tt;
+      const int kx = __ldg(s.kvec + 3 * k), ky = __ldg(s.kvec + 3 * k + 1) + ky0,
+                kz = __ldg(s.kvec + 3 * k + 2) + kz0;
+      const longlong2 o =
+          *(const longlong2*)(ek + ((size_t)wrap_slice(ifirst1 + t, M) * totk + k) * 2);
+      long long are, aim, bre, bim;
+      ewald_term_fixed(s, X, Y, Z, w, 2 * tt, kx, ky, kz, q, are, aim);
+      ewald_term_fixed(s, X, Y, Z, w, 2 * tt + 1, kx, ky, kz, q, bre, bim);
+      const long long nre = o.x + (bre - are), nim = o.y + (bim - aim);
+      *(longlong2*)(stage + ((size_t)(t - 1) * totk + k) * 2) = make_longlong2(nre, nim);
+      const double ore = __ll2double_rn(o.x) * is, oim = __ll2double_rn(o.y) * is;
+      const double rre = __ll2double_rn(nre) * is, rim = __ll2double_rn(nim) * is;
+      acc += 2 * __ldg(s.vk + k) * ((rre * rre + rim * rim) - (ore * ore + oim * oim));
+    }
+  }
+  const double sum = block_sum(acc, m.red);
+  return sum * s.one_over_2v * s.tau / s.epsilon;
 }
 
 static __device__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
@@ -548,6 +603,8 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
     double* path = P.paths + s.path_offset;
     const uint32_t att0 = P.state[r].attempt;
     double* cache = (P.nodecache && s.nc_offset >= 0) ? P.nodecache + s.nc_offset : nullptr;
+    long long* ek = (P.ekcache && s.ek_offset >= 0) ? P.ekcache + s.ek_offset : nullptr;
+    long long* ekstage = ek ? P.ekstage + (size_t)blockIdx.x * P.ekstage_stride : nullptr;
     const int np = s.npart, nsec = s.nsec, M = s.nslice, L = s.nlevel;
     for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
     const int nat = P.nattempt_r ? P.nattempt_r[r] : P.nattempt;
@@ -601,7 +658,10 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
         double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
         if (s.ewald && s.coulomb && level == 0) {
-          for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
+          if (ek)
+            ds += ewald_level0_cached(s, m, ipart, ifirst1, ek, ekstage);
+          else
+            for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
         }
         double dsn = 0.0;
         if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level, cache, ifirst1);
@@ -633,6 +693,14 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
           m.s1z[t * np + ipart] = m.mz[t];
         }
         if (threadIdx.x == 0) ++nacc;
+        if (ek) {  // the moved slices' structure factors: the staged level-0 values
+          const int totk = s.totk;
+          for (int it = threadIdx.x; it < (nsec - 2) * totk; it += blockDim.x) {
+            const int tt = it / totk, k = it - tt * totk;
+            *(longlong2*)(ek + ((size_t)wrap_slice(ifirst1 + 1 + tt, M) * totk + k) * 2) =
+                *(const longlong2*)(ekstage + (size_t)it * 2);
+          }
+        }
         if (cache && mynode) {
           // The moved slices now hold the level evaluations; the entries that
           // pair them the other way round (r2 on a moved slice) are stale.

@@ -59,6 +59,11 @@ struct DevSys {
   uint32_t stream_id;     // random stream of this replica (its replica or request id)
   long long nc_offset;    // doubles into the Slater-result cache pool (-1: no cache)
   int nc_stride;          // doubles per cache entry
+  // Structure factors rho_k = sum_j q_j e^{ik.r_j} of every path slice, kept as
+  // integers on a fixed-point grid so that incremental updates equal a fresh sum
+  // bit for bit: [nslice][totk][re, im].
+  long long ek_offset;    // int64 words into the structure-factor cache (-1: none)
+  double ek_scale;        // grid spacing 1/ek_scale (a power of two)
   long long path_offset;  // doubles into the path pool
   long long inv_offset;   // doubles into the node scratch pool (-1: shared memory)
 };

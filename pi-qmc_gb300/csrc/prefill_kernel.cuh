@@ -68,3 +68,58 @@ __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) 
 }
 
 }  // namespace pimc
+
+namespace pimc {
+
+// Structure factors rho_k = sum_j q_j e^{ik.r_j} of every slice of the given
+// replicas (EwaldSum::evalLongRange's sum over particles,
+// src/util/EwaldSum.cc:152-170), each term on the cache's fixed-point grid, so
+// the integer sum is exact and independent of the order of the terms: the
+// section kernel's incremental updates keep these bits.  One CTA per
+// (replica, slice); the bead tables of the slice in shared memory.
+struct EkPrefillParams {
+  const DevSys* sys;
+  const double* paths;
+  long long* ek;       // the structure-factor cache pool (entries at sys.ek_offset)
+  const int* slots;    // replicas to fill (null: 0 .. nslot-1)
+  int nslot;
+  int nslice_max;
+};
+
+__global__ void __launch_bounds__(kBlock) ewald_prefill_kernel(EkPrefillParams P) {
+  extern __shared__ double sh[];
+  const int k0 = blockIdx.y;
+  const int r = P.slots ? P.slots[k0] : k0;
+  const DevSys& s = P.sys[r];
+  const int t = blockIdx.x;
+  if (s.ek_offset < 0 || t >= s.nslice) return;
+  const int np = s.npart, totk = s.totk;
+  const int ky0 = s.ikmax[1], kz0 = s.ikmax[2];
+  const int nx = s.ikmax[0] + 1, ny = 2 * ky0 + 1;
+  const int w = np;
+  double2* X = (double2*)sh;
+  double2* Y = X + nx * w;
+  double2* Z = Y + ny * w;
+  double* q = (double*)(Z + (2 * kz0 + 1) * w);
+  const double* path = P.paths + s.path_offset + (size_t)t * np * 3;
+  for (int j = threadIdx.x; j < np; j += blockDim.x) {
+    ewald_bead_tables(s, X, Y, Z, w, j, path[3 * j], path[3 * j + 1], path[3 * j + 2]);
+    q[j] = s.charge[species_of(s, j)];
+  }
+  __syncthreads();
+  long long* out = P.ek + s.ek_offset + (size_t)t * totk * 2;
+  for (int k = threadIdx.x; k < totk; k += blockDim.x) {
+    const int kx = __ldg(s.kvec + 3 * k), ky = __ldg(s.kvec + 3 * k + 1) + ky0,
+              kz = __ldg(s.kvec + 3 * k + 2) + kz0;
+    long long re = 0, im = 0;
+    for (int j = 0; j < np; ++j) {
+      long long a, b;
+      ewald_term_fixed(s, X, Y, Z, w, j, kx, ky, kz, q[j], a, b);
+      re += a;
+      im += b;
+    }
+    *(longlong2*)(out + 2 * k) = make_longlong2(re, im);
+  }
+}
+
+}  // namespace pimc

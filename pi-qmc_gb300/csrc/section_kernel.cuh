@@ -581,6 +581,64 @@ static __device__ double action_partial(const DevSys& s, const Smem& m, int ipar
   return acc;
 }
 
+// e^{ik.r} factor tables of one bead, column `col` of X [nx][w], Y [ny][w] and
+// Z [nz][w] (Y and Z rows offset by ikmax): EwaldSum's recurrence over
+// multiples of the first wave vector (src/util/EwaldSum.cc:110-150), in
+// individually rounded operations, so every kernel that builds a bead's tables
+// gets the same bits.
+static __device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
+  return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                      __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+
+static __device__ void ewald_bead_tables(const DevSys& s, double2* X, double2* Y, double2* Z,
+                                         int w, int col, double x, double y, double z) {
+  const int kx0 = s.ikmax[0], ky0 = s.ikmax[1], kz0 = s.ikmax[2];
+  X[col] = make_double2(1.0, 0.0);
+  Y[ky0 * w + col] = make_double2(1.0, 0.0);
+  Z[kz0 * w + col] = make_double2(1.0, 0.0);
+  double sn, cs;
+  if (kx0 > 0) {
+    sincos(__dmul_rn(s.deltak[0], x), &sn, &cs);
+    X[w + col] = make_double2(cs, sn);
+  }
+  if (ky0 > 0) {
+    sincos(__dmul_rn(s.deltak[1], y), &sn, &cs);
+    Y[(ky0 + 1) * w + col] = make_double2(cs, sn);
+    Y[(ky0 - 1) * w + col] = make_double2(cs, -sn);
+  }
+  if (kz0 > 0) {
+    sincos(__dmul_rn(s.deltak[2], z), &sn, &cs);
+    Z[(kz0 + 1) * w + col] = make_double2(cs, sn);
+    Z[(kz0 - 1) * w + col] = make_double2(cs, -sn);
+  }
+  const double2 x1 = X[w + col];
+  for (int k = 2; k <= kx0; ++k) X[k * w + col] = cmul_rn(X[(k - 1) * w + col], x1);
+  const double2 yp = Y[(ky0 + 1) * w + col], ym = Y[(ky0 - 1) * w + col];
+  for (int k = 2; k <= ky0; ++k) {
+    Y[(ky0 + k) * w + col] = cmul_rn(Y[(ky0 + k - 1) * w + col], yp);
+    Y[(ky0 - k) * w + col] = cmul_rn(Y[(ky0 - k + 1) * w + col], ym);
+  }
+  const double2 zp = Z[(kz0 + 1) * w + col], zm = Z[(kz0 - 1) * w + col];
+  for (int k = 2; k <= kz0; ++k) {
+    Z[(kz0 + k) * w + col] = cmul_rn(Z[(kz0 + k - 1) * w + col], zp);
+    Z[(kz0 - k) * w + col] = cmul_rn(Z[(kz0 - k + 1) * w + col], zm);
+  }
+}
+
+// q e^{ik.r} of table column col for k-vector k, on the fixed-point grid of the
+// structure-factor cache (rounded to the nearest multiple of 1/ek_scale).
+static __device__ __forceinline__ void ewald_term_fixed(const DevSys& s, const double2* X,
+                                                        const double2* Y, const double2* Z,
+                                                        int w, int col, int kx, int ky, int kz,
+                                                        double q, long long& re, long long& im) {
+  const double2 a = X[kx * w + col];
+  const double2 t = make_double2(__dmul_rn(q, a.x), __dmul_rn(q, a.y));
+  const double2 v = cmul_rn(cmul_rn(t, Y[ky * w + col]), Z[kz * w + col]);
+  re = __double2ll_rn(__dmul_rn(v.x, s.ek_scale));
+  im = __double2ll_rn(__dmul_rn(v.y, s.ek_scale));
+}
+
 // EwaldSum::evalLongRange (src/util/EwaldSum.cc:103-181) for the old and the
 // new configuration of one slice (the new one has particle ipart at the moving
 // bead), as CoulombAction::getActionDifference uses them at level 0
@@ -596,53 +654,10 @@ static __device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipar
   const int w = np + 1;
   __syncthreads();
   for (int p = threadIdx.x; p < w; p += blockDim.x) {
-    double x, y, z;
-    if (p < np) {
-      x = m.s1x[t * np + p];
-      y = m.s1y[t * np + p];
-      z = m.s1z[t * np + p];
-    } else {
-      x = m.mx[t];
-      y = m.my[t];
-      z = m.mz[t];
-    }
-    X[p] = make_double2(1.0, 0.0);
-    Y[ky0 * w + p] = make_double2(1.0, 0.0);
-    Z[kz0 * w + p] = make_double2(1.0, 0.0);
-    double sn, cs;
-    if (kx0 > 0) {
-      sincos(s.deltak[0] * x, &sn, &cs);
-      X[w + p] = make_double2(cs, sn);
-    }
-    if (ky0 > 0) {
-      sincos(s.deltak[1] * y, &sn, &cs);
-      Y[(ky0 + 1) * w + p] = make_double2(cs, sn);
-      Y[(ky0 - 1) * w + p] = make_double2(cs, -sn);
-    }
-    if (kz0 > 0) {
-      sincos(s.deltak[2] * z, &sn, &cs);
-      Z[(kz0 + 1) * w + p] = make_double2(cs, sn);
-      Z[(kz0 - 1) * w + p] = make_double2(cs, -sn);
-    }
-    const double2 x1 = X[w + p];
-    for (int k = 2; k <= kx0; ++k) {
-      const double2 a = X[(k - 1) * w + p];
-      X[k * w + p] = make_double2(a.x * x1.x - a.y * x1.y, a.x * x1.y + a.y * x1.x);
-    }
-    const double2 yp = Y[(ky0 + 1) * w + p], ym = Y[(ky0 - 1) * w + p];
-    for (int k = 2; k <= ky0; ++k) {
-      double2 a = Y[(ky0 + k - 1) * w + p];
-      Y[(ky0 + k) * w + p] = make_double2(a.x * yp.x - a.y * yp.y, a.x * yp.y + a.y * yp.x);
-      a = Y[(ky0 - k + 1) * w + p];
-      Y[(ky0 - k) * w + p] = make_double2(a.x * ym.x - a.y * ym.y, a.x * ym.y + a.y * ym.x);
-    }
-    const double2 zp = Z[(kz0 + 1) * w + p], zm = Z[(kz0 - 1) * w + p];
-    for (int k = 2; k <= kz0; ++k) {
-      double2 a = Z[(kz0 + k - 1) * w + p];
-      Z[(kz0 + k) * w + p] = make_double2(a.x * zp.x - a.y * zp.y, a.x * zp.y + a.y * zp.x);
-      a = Z[(kz0 - k + 1) * w + p];
-      Z[(kz0 - k) * w + p] = make_double2(a.x * zm.x - a.y * zm.y, a.x * zm.y + a.y * zm.x);
-    }
+    if (p < np)
+      ewald_bead_tables(s, X, Y, Z, w, p, m.s1x[t * np + p], m.s1y[t * np + p], m.s1z[t * np + p]);
+    else
+      ewald_bead_tables(s, X, Y, Z, w, p, m.mx[t], m.my[t], m.mz[t]);
   }
   __syncthreads();
   double so = 0.0, sn_ = 0.0;
