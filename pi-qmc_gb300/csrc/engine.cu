@@ -960,6 +960,7 @@ int enqueue_thermo(pimc_engine* e, cudaStream_t st, int row) {
   P.sys = e->d_sys.p;
   P.index = nullptr;
   P.paths = e->d_paths.p;
+  P.ekcache = e->d_ekcache.p;
   P.partial = e->d_partial.p;
   P.nchunk = kThermoChunks;
   P.nrep = e->nrep;
@@ -1829,6 +1830,7 @@ int pimc_server_energy(pimc_engine* e, double* energy) {
   P.sys = e->d_sys.p;
   P.index = e->d_order.p;
   P.paths = e->d_pool.p;
+  P.ekcache = nullptr;  // servers take no Ewald systems
   P.partial = d_part;
   P.nchunk = nchunk;
   P.nrep = e->nactive;

@@ -96,6 +96,7 @@ struct ThermoParams {
   const DevSys* sys;
   const int* index;  // replicas to measure (null: all, blockIdx.y)
   const double* paths;
+  const long long* ekcache;  // structure factors of Ewald replicas (null: none)
   double* partial;  // [nrep][nchunk]
   int nchunk;
   int nrep;
@@ -505,7 +506,22 @@ __global__ void __launch_bounds__(kBlock) thermo_kernel(ThermoParams P) {
     }
   }
   double tot = block_sum(part, m.red);
-  if (s.coulomb && s.ewald) {
+  if (s.coulomb && s.ewald && P.ekcache && s.ek_offset >= 0) {
+    // evalLongRange of every slice from its cached structure factors:
+    // sum_k 2 v_k |rho_k|^2 / (2V) + the self energy
+    const long long* ek = P.ekcache + s.ek_offset;
+    const double is = 1.0 / s.ek_scale;
+    const int nt = max(0, t1 - t0), totk = s.totk;
+    double lr = 0.0;
+    for (int it = threadIdx.x; it < nt * totk; it += blockDim.x) {
+      const int t = t0 + it / totk, k = it % totk;
+      const longlong2 v = *(const longlong2*)(ek + ((size_t)t * totk + k) * 2);
+      const double re = __ll2double_rn(v.x) * is, im = __ll2double_rn(v.y) * is;
+      lr += 2 * __ldg(s.vk + k) * (re * re + im * im);
+    }
+    const double sum = block_sum(lr, m.red);
+    tot += (sum * s.one_over_2v + nt * s.self_energy) / s.epsilon;
+  } else if (s.coulomb && s.ewald) {
     for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
     for (int t = t0; t < t1; ++t) {
       __syncthreads();

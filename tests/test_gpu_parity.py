@@ -213,6 +213,42 @@ def test_uneven_batch_matches_checker(pimc):
         assert E[r] == pytest.approx(port.thermo_energy(), rel=1e-12)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_largest_node_species_matches_checker(pimc, precision):
+    # 32 particles per spin species, the lane-group limit (W = 32, largest
+    # Slater scratch), SHONodes at the serving workload's node temperature.
+    from pimc_gb300 import workloads as WL
+    kw = dict(counts=[32, 32], sho_omega=[1.0, 1.0], nslice=64, beta=64 / 25.6, nlevel=3,
+              coulomb=1, norder=3, node_kind=[1, 1], node_omega=[1.0, 1.0],
+              node_temperature=0.25, cell=WL.DOT_CELL)
+    tabs, _ = pimc.coulomb_tables(kw)
+    path = W.initial_path(O.make_config(**kw), "const", seed=41)
+    e = pimc.Engine(kw, 2, tabs, None, seed=5, precision=precision)
+    e.upload_paths([path, path])
+    n = 40
+    rec = e.run_sections(n, records=True)
+    out = e.download_paths()
+    for r in range(2):
+        port = O.PortOracle(O.make_config(**dict(kw, seed=5, replica=r)), tabs, None)
+        port.set_path(path)
+        pr = port.run(n)
+        if precision == 0:
+            assert np.array_equal(pr["reject_level"], rec["reject_level"][r])
+            assert np.array_equal(pr["ipart"], rec["ipart"][r])
+            assert rel_close(pr["ds"], rec["ds"][r][:, :9], 1e-12)
+            # 32 x 32 SHO Slater matrices: condition numbers ~1e8, so the node
+            # terms agree with the checker's LAPACK-order LU to ~1e-8
+            assert rel_close(pr["ds_node"], rec["ds_node"][r][:, :9], 1e-6)
+            assert np.abs(port.get_path() - out[r]).max() <= 1e-12
+        else:
+            # the mixed form draws other proposals: same particles and
+            # sections, a valid chain (finite action differences)
+            assert np.array_equal(pr["ipart"], rec["ipart"][r])
+            assert np.all(np.isfinite(rec["ds"][r][:, :5]))
+    acc, att, st = e.replica_status()
+    assert np.all(att == n) and np.all(st == 0)
+
+
 def test_graph_steps_equal_direct_calls(pimc):
     # The captured step graph (sweep + energy measurement, replayed) is the same
     # work as the direct calls: energies and paths bit for bit, and a replay
