@@ -119,6 +119,7 @@ struct pimc_engine {
   DevBuf<double> d_paths;
   DevBuf<double> d_nodescr;
   DevBuf<double> d_nodecache;
+  DevBuf<double> d_prefill_scr;  // global Slater scratch of the cache fill (large matrices)
   DevBuf<long long> d_ekcache;  // structure factors per replica and slice
   DevBuf<long long> d_ekstage;  // per-CTA staging of an attempt's new structure factors
   int ekstage_stride = 0;       // int64 words per CTA
@@ -172,6 +173,7 @@ struct pimc_engine {
     d_nodescr.free();
     d_nodecache.free();
     d_ekcache.free();
+    d_prefill_scr.free();
     d_ekstage.free();
     d_order.free();
     d_next.free();
@@ -768,12 +770,24 @@ int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) 
   P.ntask_per_slot = nsp * mmax;
   P.stage_stride = (6 * nmax + 1) & ~1;
   P.scratch_stride = (node_group_scratch(nmax, anyfree) + 1) & ~1;
-  const size_t per_warp = (size_t)(P.stage_stride + P.scratch_stride) * 8;
-  const int nw = (int)std::max<size_t>(1, std::min<size_t>(kBlock / 32, (200 * 1024) / per_warp));
+  // Slater scratch in shared memory up to 6 KB a warp, else in global memory
+  const bool gscr = P.scratch_stride * 8 > 6 * 1024;
+  const int nw = kBlock / 32;
+  const size_t smem = (size_t)nw * (P.stage_stride + (gscr ? 0 : P.scratch_stride)) * 8;
+  const long long ntask = (long long)nslot * P.ntask_per_slot;
+  const int grid = (int)std::min<long long>((ntask + nw - 1) / nw, (long long)e->num_sms * 4);
+  P.gscratch = nullptr;
+  if (gscr) {
+    const size_t need = (size_t)grid * nw * P.scratch_stride;
+    if (e->d_prefill_scr.n < need) {
+      CU(cudaStreamSynchronize(e->stream));  // an earlier fill may still use it
+      if (e->d_prefill_scr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc prefill scratch");
+    }
+    P.gscratch = e->d_prefill_scr.p;
+  }
   cudaFuncSetAttribute(cache_prefill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        200 * 1024);
-  const dim3 grid((P.ntask_per_slot + nw - 1) / nw, nslot);
-  cache_prefill_kernel<<<grid, 32 * nw, per_warp * nw, e->stream>>>(P);
+  cache_prefill_kernel<<<grid, kBlock, smem, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
   return PIMC_OK;

@@ -104,23 +104,24 @@ __device__ __forceinline__ void pbc(const DevSys& s, double& x, double& y, doubl
 __device__ __forceinline__ double pg_eval(double nome, double pref, double k, int nmax, double x,
                                           double* grad) {
   double sw, cw;
-  sincos(k * x, &sw, &cw);
+  sincos(__dmul_rn(k, x), &sw, &cw);
+  // (rounded operations throughout: every call site computes the same bits)
   double tr = 1.0, ti = 0.0;  // term
   double s0r = 0.0, s1r = 0.0;
   double nomeN = 1.0;
   for (int n = 1; n < nmax; ++n) {
-    const double f = nomeN * nomeN * nome;
-    const double fr = f * cw, fi = f * sw;
-    const double nr = tr * fr - ti * fi;
-    const double ni = tr * fi + ti * fr;
+    const double f = __dmul_rn(__dmul_rn(nomeN, nomeN), nome);
+    const double fr = __dmul_rn(f, cw), fi = __dmul_rn(f, sw);
+    const double nr = __dsub_rn(__dmul_rn(tr, fr), __dmul_rn(ti, fi));
+    const double ni = __dadd_rn(__dmul_rn(tr, fi), __dmul_rn(ti, fr));
     tr = nr;
     ti = ni;
-    s0r += tr;
-    s1r += (-ti * k) * double(n);  // real(term * i k * n)
-    nomeN *= nome;
+    s0r = __dadd_rn(s0r, tr);
+    s1r = __dadd_rn(s1r, __dmul_rn(__dmul_rn(-ti, k), double(n)));  // real(term * i k * n)
+    nomeN = __dmul_rn(nomeN, nome);
   }
-  *grad = pref * 2 * s1r;
-  return pref * (1 + 2 * s0r);
+  *grad = __dmul_rn(__dmul_rn(pref, 2.0), s1r);
+  return __dmul_rn(pref, __dadd_rn(1.0, __dmul_rn(2.0, s0r)));
 }
 
 // Pair-action table lookup on the logarithmic grid

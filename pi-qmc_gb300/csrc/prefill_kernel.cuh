@@ -20,50 +20,61 @@ struct PrefillParams {
   int ntask_per_slot;  // nspecies_max x nslice_max
   int stage_stride;    // doubles of slice-pair staging per warp (6 n_max)
   int scratch_stride;  // doubles of Slater scratch per warp
+  double* gscratch;    // per-warp Slater scratch in global memory (null: shared memory)
 };
 
+// Warps loop over the (slot, species, slice) entries; shared memory holds each
+// warp's staged slice pair, and its Slater scratch too unless that is large
+// (27 x 27 free-particle matrices: 35 KB a warp), when the scratch lives in
+// global memory so that more warps stay resident.
 __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) {
   extern __shared__ double sh[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int k = blockIdx.y;
-  const int r = P.slots ? P.slots[k] : k;
-  const DevSys& s = P.sys[r];
-  const int task = blockIdx.x * nwarps + warp;
-  if (task >= P.ntask_per_slot || s.nc_offset < 0) return;  // warp-uniform
-  const int M = s.nslice, sp = task / M, t = task % M;
-  if (sp >= s.nspecies || t >= M || !s.node_kind[sp]) return;
-  const int n = s.spec_count[sp], f = s.spec_first[sp], np = s.npart;
-  const double* path = P.paths + s.path_offset;
-  double* e = P.cache + s.nc_offset + ((size_t)sp * M + t) * s.nc_stride;
-  const double scale = P.state[r].node_scale[sp];
-  const double ep = (double)P.state[r].epoch[sp];
-  double* st = sh + (size_t)warp * (P.stage_stride + P.scratch_stride);
-  double* scr = st + P.stage_stride;
-  // stage the species' beads of slices t (r1) and t + M/2 (r2)
-  const int t2 = (t + M / 2) % M;
-  for (int p = lane; p < n; p += 32) {
-    const double* b1 = path + ((size_t)t * np + f + p) * 3;
-    const double* b2 = path + ((size_t)t2 * np + f + p) * 3;
-    st[p] = b1[0];
-    st[n + p] = b1[1];
-    st[2 * n + p] = b1[2];
-    st[3 * n + p] = b2[0];
-    st[4 * n + p] = b2[1];
-    st[5 * n + p] = b2[2];
-  }
-  __syncwarp();
-  // node_eval_group reads particle f + p: views offset so that it lands on entry p
-  SliceView v1{st - f, st + n - f, st + 2 * n - f, n, 0, -1, 0, 0, 0};
-  SliceView v2{st + 3 * n - f, st + 4 * n - f, st + 5 * n - f, n, 0, -1, 0, 0, 0};
-  double det = 0;
-  int err = 0;
-  node_eval_group<32>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err, e + 2,
-                      e + 2 + n, nullptr, 0xffffffffu);
-  __syncwarp();
-  if (lane == 0) {
-    e[1] = det;
-    e[0] = err ? __longlong_as_double(0x7ff8000000000000LL) : ep;
-    e[cache_mask_slot(s, sp)] = 0.0;
+  const long long gw = (long long)blockIdx.x * nwarps + warp;
+  const long long nwt = (long long)gridDim.x * nwarps;
+  double* st = sh + (size_t)warp * P.stage_stride;
+  double* scr = P.gscratch ? P.gscratch + gw * P.scratch_stride
+                           : sh + (size_t)nwarps * P.stage_stride + (size_t)warp * P.scratch_stride;
+  const long long ntask = (long long)P.nslot * P.ntask_per_slot;
+  for (long long task = gw; task < ntask; task += nwt) {  // warp-uniform
+    const int k = (int)(task / P.ntask_per_slot), tk = (int)(task % P.ntask_per_slot);
+    const int r = P.slots ? P.slots[k] : k;
+    const DevSys& s = P.sys[r];
+    if (s.nc_offset < 0) continue;
+    const int M = s.nslice, sp = tk / M, t = tk % M;
+    if (sp >= s.nspecies || !s.node_kind[sp]) continue;
+    const int n = s.spec_count[sp], f = s.spec_first[sp], np = s.npart;
+    const double* path = P.paths + s.path_offset;
+    double* e = P.cache + s.nc_offset + ((size_t)sp * M + t) * s.nc_stride;
+    const double scale = P.state[r].node_scale[sp];
+    const double ep = (double)P.state[r].epoch[sp];
+    // stage the species' beads of slices t (r1) and t + M/2 (r2)
+    const int t2 = (t + M / 2) % M;
+    __syncwarp();
+    for (int p = lane; p < n; p += 32) {
+      const double* b1 = path + ((size_t)t * np + f + p) * 3;
+      const double* b2 = path + ((size_t)t2 * np + f + p) * 3;
+      st[p] = b1[0];
+      st[n + p] = b1[1];
+      st[2 * n + p] = b1[2];
+      st[3 * n + p] = b2[0];
+      st[4 * n + p] = b2[1];
+      st[5 * n + p] = b2[2];
+    }
+    __syncwarp();
+    // node_eval_group reads particle f + p: views offset so that it lands on entry p
+    SliceView v1{st - f, st + n - f, st + 2 * n - f, n, 0, -1, 0, 0, 0};
+    SliceView v2{st + 3 * n - f, st + 4 * n - f, st + 5 * n - f, n, 0, -1, 0, 0, 0};
+    double det = 0;
+    int err = 0;
+    node_eval_group<32>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err, e + 2,
+                        e + 2 + n, nullptr, 0xffffffffu);
+    __syncwarp();
+    if (lane == 0) {
+      e[1] = det;
+      e[0] = err ? __longlong_as_double(0x7ff8000000000000LL) : ep;
+      e[cache_mask_slot(s, sp)] = 0.0;
+    }
   }
 }
 

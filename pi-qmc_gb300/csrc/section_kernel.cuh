@@ -99,79 +99,89 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   double* G = R + n + 1;    // 3 n*n gradient factors (free-particle nodes)
   const bool sho = s.node_kind[sp] == 1;
   // --- build the Slater matrix: A(i,j) = scale * rho(r1_j, r2_i)
-  if (gl < n) {
-    double rix, riy, riz;
-    v2.get(f + gl, rix, riy, riz);
-    // rows to recompute (the others come from ecache): every row unless the
-    // cached matrix is valid apart from the rows in rowmask
-    const bool row_new = (rowmask >> gl) & 1u;
+  // Elements come from ecache where it holds them (a column update keeps every
+  // column but jcol; a row refresh keeps the rows outside rowmask); the others
+  // are computed.  Whole rows (all of them without a cache, the stale ones on a
+  // refresh) go one element per lane and step, so that refreshing one or two
+  // rows still spreads over the group; the new column of a column update goes
+  // one row per lane.  Every element is the same rounded arithmetic wherever
+  // it is computed, so cached and recomputed values agree bit for bit.
+  const int nn = n * n;
+  const unsigned nmask = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+  const unsigned rows_new = !ecache ? nmask : (jcol < 0 ? (rowmask & nmask) : 0u);
+  // element (i, j): value into A (scaled), E (SHO) or G (gradients), and into
+  // ecache (a refresh) or newcol (the new column) when this group writes
+  auto element = [&](int i, int j) {
+    double rix, riy, riz, rjx, rjy, rjz;
+    v2.get(f + i, rix, riy, riz);
+    v1.get(f + j, rjx, rjy, rjz);
+    const bool to_cache = ecache && jcol < 0 && write;
+    const bool to_col = newcol && j == jcol && write;
     if (sho) {
-      const double c = s.node_c[sp], ch = s.node_cosh[sp];
       const double ri2 = dot3(rix, riy, riz, rix, riy, riz);
-      for (int j = 0; j < n; ++j) {
-        double e;
-        if (ecache && ((jcol >= 0 && j != jcol) || (jcol < 0 && !row_new))) {
-          e = ecache[j * n + gl];
-        } else {
-          double rjx, rjy, rjz;
-          v1.get(f + j, rjx, rjy, rjz);
-          const double rj2 = dot3(rjx, rjy, rjz, rjx, rjy, rjz);
-          const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
-          e = exp(-c * ((ri2 + rj2) * ch - 2.0 * rirj));
-          if (ecache && jcol < 0 && write) ecache[j * n + gl] = e;
-          if (newcol && j == jcol && write) newcol[gl] = e;
-        }
-        E[j * n + gl] = e;
-        A[j * n + gl] = scale * e;
-      }
+      const double rj2 = dot3(rjx, rjy, rjz, rjx, rjy, rjz);
+      const double rirj = dot3(rix, riy, riz, rjx, rjy, rjz);
+      const double q = __dsub_rn(__dmul_rn(__dadd_rn(ri2, rj2), s.node_cosh[sp]),
+                                 __dmul_rn(2.0, rirj));
+      const double e = exp(__dmul_rn(-s.node_c[sp], q));
+      if (to_cache) ecache[j * n + i] = e;
+      if (to_col) newcol[i] = e;
+      E[j * n + i] = e;
+      A[j * n + i] = scale * e;
     } else {
-      // values rho = v0 v1 v2 and, for the distances, the gradient of each
-      // element with respect to r1_j (the r2_i gradient is its negative); a
-      // column update reads the unchanged columns from ecache ([4][n][n]:
-      // values, then the three gradient components)
-      const int nn = n * n;
-      for (int j = 0; j < n; ++j) {
-        double val, gx, gy, gz;
-        if (ecache && ((jcol >= 0 && j != jcol) || (jcol < 0 && !row_new))) {
-          val = ecache[j * n + gl];
-          gx = ecache[nn + j * n + gl];
-          gy = ecache[2 * nn + j * n + gl];
-          gz = ecache[3 * nn + j * n + gl];
-        } else {
-          double rjx, rjy, rjz;
-          v1.get(f + j, rjx, rjy, rjz);
-          double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
-          pbc(s, dx, dy, dz);
-          double g0, g1, g2;
-          const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
-          const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
-          const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
-          val = v0 * v1v * v2v;
-          gx = g0 / (v0 + 1e-300);
-          gy = g1 / (v1v + 1e-300);
-          gz = g2 / (v2v + 1e-300);
-          gx *= v0; gy *= v0; gz *= v0;
-          gx *= v1v; gy *= v1v; gz *= v1v;
-          gx *= v2v; gy *= v2v; gz *= v2v;
-          if (ecache && jcol < 0 && write) {
-            ecache[j * n + gl] = val;
-            ecache[nn + j * n + gl] = gx;
-            ecache[2 * nn + j * n + gl] = gy;
-            ecache[3 * nn + j * n + gl] = gz;
-          }
-          if (newcol && j == jcol && write) {
-            newcol[gl] = val;
-            newcol[n + gl] = gx;
-            newcol[2 * n + gl] = gy;
-            newcol[3 * n + gl] = gz;
-          }
-        }
-        A[j * n + gl] = scale * val;
-        G[j * n + gl] = gx;
-        G[nn + j * n + gl] = gy;
-        G[2 * nn + j * n + gl] = gz;
+      double dx = rjx - rix, dy = rjy - riy, dz = rjz - riz;
+      pbc(s, dx, dy, dz);
+      double g0, g1, g2;
+      const double v0 = pg_eval(s.pg_nome[sp][0], s.pg_pref[sp][0], s.pg_k[sp][0], s.pg_nmax[sp][0], dx, &g0);
+      const double v1v = pg_eval(s.pg_nome[sp][1], s.pg_pref[sp][1], s.pg_k[sp][1], s.pg_nmax[sp][1], dy, &g1);
+      const double v2v = pg_eval(s.pg_nome[sp][2], s.pg_pref[sp][2], s.pg_k[sp][2], s.pg_nmax[sp][2], dz, &g2);
+      const double val = v0 * v1v * v2v;
+      double gx = g0 / (v0 + 1e-300), gy = g1 / (v1v + 1e-300), gz = g2 / (v2v + 1e-300);
+      gx *= v0; gy *= v0; gz *= v0;
+      gx *= v1v; gy *= v1v; gz *= v1v;
+      gx *= v2v; gy *= v2v; gz *= v2v;
+      if (to_cache) {
+        ecache[j * n + i] = val;
+        ecache[nn + j * n + i] = gx;
+        ecache[2 * nn + j * n + i] = gy;
+        ecache[3 * nn + j * n + i] = gz;
+      }
+      if (to_col) {
+        newcol[i] = val;
+        newcol[n + i] = gx;
+        newcol[2 * n + i] = gy;
+        newcol[3 * n + i] = gz;
+      }
+      A[j * n + i] = scale * val;
+      G[j * n + i] = gx;
+      G[nn + j * n + i] = gy;
+      G[2 * nn + j * n + i] = gz;
+    }
+  };
+  // cached rows (with the new column of a column update), one row per lane
+  if (ecache && gl < n && !((rows_new >> gl) & 1u)) {
+    const int i = gl;
+    for (int j = 0; j < n; ++j) {
+      if (jcol >= 0 && j == jcol) {
+        element(i, j);
+      } else if (sho) {
+        const double e = ecache[j * n + i];
+        E[j * n + i] = e;
+        A[j * n + i] = scale * e;
+      } else {
+        A[j * n + i] = scale * ecache[j * n + i];
+        G[j * n + i] = ecache[nn + j * n + i];
+        G[nn + j * n + i] = ecache[2 * nn + j * n + i];
+        G[2 * nn + j * n + i] = ecache[3 * nn + j * n + i];
       }
     }
+  }
+  // rows computed in full, one element per lane and step
+  const int nrows = __popc(rows_new);
+  for (int e = gl; e < nrows * n; e += W) {
+    unsigned rm = rows_new;
+    for (int q = e / n; q > 0; --q) rm &= rm - 1u;  // drop the first e/n set rows
+    element(__ffs(rm) - 1, e % n);
   }
   __syncwarp();
   // --- LU with partial pivoting (the pivot is the first largest |a|)
