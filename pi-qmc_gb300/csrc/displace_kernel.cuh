@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
           const int n = s.spec_count[sp], f = s.spec_first[sp];
           const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
           const int W = node_group_width(n), G = 32 / W, g = lane / W, gl = lane & (W - 1);
-          double* gscr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
+          double* gscr = group_scr(m, warp, g, n, !sho);
+          double* gcold = group_cold(m, warp, g, n, !sho);
           double* st = smem + P.stage_off + (size_t)(warp * G + g) * 6 * n;  // [2][3][n]
           if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
           __syncthreads();
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
                 int err = 0;
                 const bool store = act && !hit;
                 node_eval_dispatch(W, s, sp, v1, v2, scale[sp], gscr, 1, nullptr, -1, store, det,
-                                   err, d1, d2);
+                                   err, d1, d2, nullptr, 0xffffffffu, gcold);
                 if (store && gl == 0) {
                   if (pass == 0) ndet[t] = det;
                   if (err) atomicOr(&m.ictl[C_FLAG], 1);

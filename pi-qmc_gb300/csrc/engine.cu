@@ -104,6 +104,7 @@ struct DevBuf {
 // Layout choices the autotuner varies.
 struct LayoutOpts {
   bool scratch_global = false;  // per-warp Slater scratch in global memory even when it fits
+  bool full_ewald_tables = false;  // Ewald tables for every bead (full evalLongRange sums)
 };
 
 struct pimc_engine {
@@ -327,15 +328,35 @@ int cache_entry_doubles(const DevSys& d) {
   return (2 + 2 * n + n * n * (free_nodes ? 4 : 1) + 2) & ~1;  // + the stale-row word
 }
 
+// Fixed-point exponent of a replica's structure-factor cache, or -1 when it
+// has none (no Ewald sum; fixed-node sections that can overlap; charges too
+// large for a fine grid): |rho_k| <= sum |q|, and an update adds at most
+// 2 max|q| more, so 60 bits cover 3 sum |q|.
+int ek_bits(const DevSys& d) {
+  if (!(d.ewald && d.coulomb && d.totk > 0)) return -1;
+  if (d.fixed_node && !((1 << d.nlevel) < d.nslice / 2)) return -1;
+  double qsum = 0;
+  for (int i = 0; i < d.nspecies; ++i) qsum += std::fabs(d.charge[i]) * d.spec_count[i];
+  const int ebits = 60 - (int)std::ceil(std::log2(std::max(qsum, 1.0)) + 1e-9);
+  return ebits < 24 ? -1 : ebits;
+}
+
+// Dynamic shared memory of the section-sized kernels (bytes; the opt-in
+// maximum is 227 KB, less the kernels' few KB of static shared memory).
+constexpr int kSmemLimit = 220 * 1024;
+
 Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutOpts opts = {}) {
-  int nsec = 0, np = 0, nsm = 1, ewt = 0;
-  bool fixed = false;
+  int nsec = 0, np = 0, nsm = 1, per = 0;
+  bool fixed = false, ewald_full = false;
   for (const DevSys& d : sys) {
     nsec = std::max(nsec, d.nsec);
     np = std::max(np, d.npart);
     nsm = std::max(nsm, d.ns_max);
     fixed |= d.fixed_node != 0;
-    if (d.ewald) ewt = std::max(ewt, 2 * (d.ikmax[0] + 1 + 2 * d.ikmax[1] + 1 + 2 * d.ikmax[2] + 1) * (d.npart + 1));
+    if (d.ewald) {
+      per = std::max(per, d.ikmax[0] + 1 + 2 * d.ikmax[1] + 1 + 2 * d.ikmax[2] + 1);
+      ewald_full |= opts.full_ewald_tables || ek_bits(d) < 0;
+    }
   }
   Layout L{};
   int off = 0;
@@ -344,6 +365,10 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
     off += (n + 1) & ~1;  // keep 16-byte alignment
     return o;
   };
+  // Ewald tables: every bead of a slice for a full evalLongRange, or 16 bead
+  // columns (8 slices' old and new moving bead) when every Ewald replica keeps
+  // its structure factors
+  L.ewt_cols = per ? (ewald_full ? np + 1 : std::min(np + 1, 16)) : 0;
   L.s1 = take(3 * nsec * np);
   L.s2 = take(fixed ? 3 * nsec * np : 0);
   L.mv = take(3 * nsec);
@@ -355,7 +380,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.edet = take(nsec);
   L.dist = take(fixed ? nsec * 2 * nsm : 0);
   L.ndist = take(fixed ? nsec * 2 * nsm : 0);
-  L.ewt = take(ewt);
+  L.ewt = take(2 * per * L.ewt_cols);
   L.ictl = take((C_NCTL + 2 * nsec + 1) / 2 + 1);
   bool sho = false;
   for (const DevSys& d : sys)
@@ -371,41 +396,64 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   for (const DevSys& d : sys)
     for (int i = 0; i < d.nspecies; ++i) anyfree_col |= d.node_kind[i] == PIMC_NODES_FREE;
   L.ncol_stride = nsm * (anyfree_col ? 4 : 1);
-  L.ncol = fixed ? take(nsec * L.ncol_stride) : -1;
-  // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n) doubles
-  int stride = 0;
-  // (the node species present decide it: a smaller species packs more lane
-  // groups per warp, so its per-warp scratch can be the larger one)
+  const int ncol_size = fixed ? nsec * L.ncol_stride : 0;
+  // per-warp Slater scratch: (32 / W) lane groups of node_group_scratch(n)
+  // doubles, or of its hot and cold parts apart (the species present decide
+  // it: a smaller species packs more lane groups per warp)
+  int full = 0, hot = 0, cold = 0;
   for (const DevSys& d : sys)
     for (int i = 0; i < d.nspecies; ++i)
       if (d.node_kind[i]) {
-        const int n = d.spec_count[i];
-        stride = std::max(stride, (32 / node_group_width(n)) *
-                                      node_group_scratch(n, d.node_kind[i] == PIMC_NODES_FREE));
+        const int n = d.spec_count[i], G = 32 / node_group_width(n);
+        const bool fr = d.node_kind[i] == PIMC_NODES_FREE;
+        full = std::max(full, G * node_group_scratch(n, fr));
+        hot = std::max(hot, G * node_group_hot(n));
+        cold = std::max(cold, G * node_group_cold(n, fr));
       }
-  L.nodescr_stride = (stride + 1) & ~1;
-  const int need = off + nwarps * L.nodescr_stride;
-  const int limit = 200 * 1024 / 8;
-  if (need <= limit && !(opts.scratch_global && fixed)) {
-    L.nodescr = take(nwarps * L.nodescr_stride);
-    L.nodescr_in_smem = 1;
+  full = (full + 1) & ~1;
+  hot = (hot + 1) & ~1;
+  cold = (cold + 1) & ~1;
+  const int limit = kSmemLimit / 8;
+  const int base = off;
+  // placements, best first: everything in shared memory; the LU and inverse
+  // in shared memory with the cold parts (and then the new-column buffer) in
+  // the CTA's global area; all of the scratch in global memory
+  enum { kAll, kHotCol, kHot, kGlobalCol, kGlobal };
+  int place = kGlobal;
+  if (!fixed) {
+    place = kAll;
   } else {
-    L.nodescr = -1;
-    L.nodescr_in_smem = 0;
+    const int cand[5][3] = {  // {ncol in smem, per-warp scratch in smem, split}
+        {1, full, 0}, {1, hot, 1}, {0, hot, 1}, {1, 0, 0}, {0, 0, 0}};
+    for (int c = opts.scratch_global ? kGlobalCol : kAll; c <= kGlobal; ++c)
+      if (base + (cand[c][0] ? ncol_size : 0) + nwarps * cand[c][1] <= limit || c == kGlobal) {
+        place = c;
+        break;
+      }
   }
+  const bool ncol_smem = place == kAll || place == kHotCol || place == kGlobalCol;
+  L.ncol = (fixed && ncol_smem) ? take(ncol_size) : -1;
+  L.ncol_global = fixed && !ncol_smem;
+  L.split = place == kHotCol || place == kHot;
+  L.nodescr_in_smem = place == kAll || L.split;
+  L.nodescr_stride = place == kAll ? full : (L.split ? hot : full);
+  L.nodecold_stride = L.split ? cold : 0;
+  L.nodescr = L.nodescr_in_smem ? take(nwarps * L.nodescr_stride) : -1;
+  const int gwarp = L.split ? cold : (L.nodescr_in_smem ? 0 : full);
+  L.gcta = nwarps * gwarp + (L.ncol_global ? ncol_size : 0);
   L.total = off;
   ok = L.total <= limit;
   return L;
 }
 
 void set_smem_caps() {
-  section_smem_cap_v1(200 * 1024);
-  section_smem_cap_v2(200 * 1024);
-  section_smem_cap_v3(200 * 1024);
-  section_smem_cap_v4(200 * 1024);
-  cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  section_smem_cap_v1(kSmemLimit);
+  section_smem_cap_v2(kSmemLimit);
+  section_smem_cap_v3(kSmemLimit);
+  section_smem_cap_v4(kSmemLimit);
+  cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
   cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       200 * 1024);
+                       kSmemLimit);
 }
 
 // Shared memory of the estimator kernels: one staged slice (in the section
@@ -440,6 +488,8 @@ Layout estimator_layout(const std::vector<DevSys>& sys, const int* ikmax_extra) 
   L.ecache = L.ncol = -1;
   L.nodescr = 0;
   L.nodescr_in_smem = 1;
+  L.ewt_cols = np + 1;
+  L.split = L.ncol_global = L.gcta = L.nodecold_stride = 0;
   L.total = off;
   return L;
 }
@@ -606,14 +656,10 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
   occ = std::max(occ, 1);
   e->grid = std::min(nrep, nsm * occ);
-  if (!e->lay.nodescr_in_smem) {
-    for (DevSys& d : e->hsys) d.inv_offset = 0;
-    if (e->d_nodescr.alloc((size_t)e->grid * (e->block / 32) * e->lay.nodescr_stride)) {
-      delete e;
-      return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
-    }
-  } else {
-    for (DevSys& d : e->hsys) d.inv_offset = -1;
+  for (DevSys& d : e->hsys) d.inv_offset = e->lay.gcta > 0 ? 0 : -1;
+  if (e->lay.gcta > 0 && e->d_nodescr.alloc((size_t)e->grid * e->lay.gcta)) {
+    delete e;
+    return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
   }
   // Slater-result cache: per replica, per species, per path slice.  Left out
   // when the two sections of an attempt can overlap (2^L >= M/2).
@@ -1112,10 +1158,10 @@ int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmovi
     if (d.fixed_node && (d.nslice % 2)) return fail(PIMC_ERR_INVALID, "odd nslice");
   }
   if (nattempt == 0) return PIMC_OK;
-  // shared memory: the section layout (slices staged for the Ewald sums, the
+  // shared memory: a section layout (slices staged for the Ewald sums, the
   // reduction buffer, charges, control words, Slater scratch) plus a slice-pair
   // staging area per lane group
-  const int nwarps = e->block / 32;
+  const int dthreads = std::min(e->block, kBlock), nwarps = dthreads / 32;
   int stage = 0, half_max = 1, nsm = 1;
   for (const DevSys& d : e->hsys) {
     half_max = std::max(half_max, d.nslice / 2);
@@ -1126,10 +1172,24 @@ int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmovi
         stage = std::max(stage, (32 / node_group_width(n)) * 6 * n);
       }
   }
-  const Layout L = e->lay;
+  // (full Ewald tables: every slice's evalLongRange is summed here)
+  LayoutOpts dopt;
+  dopt.full_ewald_tables = true;
+  bool lok = false;
+  Layout L = make_layout(e->hsys, nwarps, lok, dopt);
+  if (!lok || (size_t)(L.total + nwarps * stage) * 8 > (size_t)kSmemLimit) {
+    dopt.scratch_global = true;
+    L = make_layout(e->hsys, nwarps, lok, dopt);
+  }
   const int stage_off = L.total;
   const size_t smem = (size_t)(L.total + nwarps * stage) * 8;
-  if (smem > 200 * 1024) return fail(PIMC_ERR_CAPACITY, "displacement working set too large");
+  if (!lok || smem > (size_t)kSmemLimit)
+    return fail(PIMC_ERR_CAPACITY, "displacement working set too large");
+  if ((size_t)e->grid * L.gcta > e->d_nodescr.n) {
+    CU(cudaStreamSynchronize(e->stream));
+    if (e->d_nodescr.alloc((size_t)e->grid * L.gcta))
+      return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
+  }
   const long long sstride = (long long)half_max * (1 + 4 * nsm);
   const size_t need = (size_t)e->grid * sstride;
   if (e->d_dscratch.n < need && e->d_dscratch.alloc(need))
@@ -1160,9 +1220,9 @@ int pimc_run_displace(pimc_engine* e, int nattempt, const double* box, int nmovi
   P.species = species;
   P.lay = L;
   P.stage_off = stage_off;
-  cudaFuncSetAttribute(displace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(displace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  displace_kernel<<<e->grid, std::min(e->block, kBlock), smem, e->stream>>>(P);
+  displace_kernel<<<e->grid, dthreads, smem, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
   // displaced paths: every slice's structure factors are rebuilt
@@ -1283,6 +1343,13 @@ int pimc_action_difference(pimc_engine* e, int level, int nbatch, const double* 
   if (level < 0 || level > s.nlevel) return fail(PIMC_ERR_INVALID, "level out of range");
   for (int b = 0; b < nbatch; ++b)
     if (ipart[b] < 0 || ipart[b] >= s.npart) return fail(PIMC_ERR_INVALID, "ipart out of range");
+  // the section layout with every bead's Ewald tables and no Slater scratch
+  LayoutOpts aopt;
+  aopt.scratch_global = true;
+  aopt.full_ewald_tables = true;
+  bool lok = false;
+  const Layout alay = make_layout(e->hsys, kBlock / 32, lok, aopt);
+  if (!lok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
   const size_t nsecd = (size_t)nbatch * s.nsec * s.npart * 3, nmovd = (size_t)nbatch * s.nsec * 3;
   double *d_sec = nullptr, *d_mov = nullptr, *d_ds = nullptr;
   int* d_ip = nullptr;
@@ -1300,8 +1367,8 @@ int pimc_action_difference(pimc_engine* e, int level, int nbatch, const double* 
   P.ipart = d_ip;
   P.ds = d_ds;
   P.level = level;
-  P.lay = e->lay;
-  action_diff_kernel<<<nbatch, kBlock, e->lay.total * 8, e->stream>>>(P);
+  P.lay = alay;
+  action_diff_kernel<<<nbatch, kBlock, P.lay.total * 8, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(ds, d_ds, nbatch * 8, cudaMemcpyDeviceToHost, e->stream));
@@ -1417,8 +1484,8 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
   occ = std::max(occ, 1);
   if (ctas_cap > 0) occ = std::min(occ, ctas_cap);
   const int grid = std::min(e->nrep, e->num_sms * occ);
-  if (!L.nodescr_in_smem) {
-    const size_t need = (size_t)grid * (block / 32) * L.nodescr_stride;
+  if (L.gcta > 0) {
+    const size_t need = (size_t)grid * L.gcta;
     if (need > e->d_nodescr.n) {
       CU(cudaStreamSynchronize(e->stream));
       if (e->d_nodescr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
@@ -1453,7 +1520,7 @@ int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg) {
 int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg) {
   if (!e || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
   cfg->block = e->block;
-  cfg->scratch_global = e->lay.nodescr_in_smem ? 0 : 1;
+  cfg->scratch_global = e->lay_opts.scratch_global ? 1 : 0;
   cfg->ctas_per_sm = e->ctas_cap;
   cfg->regs_variant = e->minb;
   cfg->ms = 0.f;
@@ -1600,8 +1667,8 @@ int refresh_order(pimc_engine* e) {
     int occ = 1;
     occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
     e->grid = std::min(e->nactive, e->num_sms * std::max(occ, 1));
-    if (!e->lay.nodescr_in_smem) {
-      const size_t need = (size_t)e->grid * (e->block / 32) * e->lay.nodescr_stride;
+    if (e->lay.gcta > 0) {
+      const size_t need = (size_t)e->grid * e->lay.gcta;
       if (need > e->d_nodescr.n) {
         CU(cudaStreamSynchronize(e->stream));
         if (e->d_nodescr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc node scratch");
@@ -1753,7 +1820,7 @@ int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_ta
   d.stream_id = stream_id;
   d.path_offset = po;
   d.nc_offset = cache ? po + pw : -1;
-  d.inv_offset = e->lay.nodescr_in_smem ? -1 : 0;
+  d.inv_offset = e->lay.gcta > 0 ? 0 : -1;
   e->hsys[r] = d;
   e->hdesc[r] = *sys;
   e->slot_path[r] = po;

@@ -12,8 +12,13 @@ struct Layout {
   int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
   int ncol_stride;
   int nrm;  // the attempt's normals, 3 per movable slice
-  int nodescr_in_smem;
-  int nodescr_stride;
+  int nodescr_in_smem;  // the node scratch (its hot parts when split) in shared memory
+  int nodescr_stride;   // doubles per warp of that scratch
+  int split;            // cold parts apart, in the CTA's global area
+  int nodecold_stride;  // doubles per warp of the cold parts
+  int ncol_global;      // the new-column buffer in the CTA's global area
+  int gcta;             // doubles of global scratch per CTA
+  int ewt_cols;         // bead columns of the Ewald tables area
   int total;  // doubles
 };
 
@@ -59,13 +64,20 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.ewt = base + L.ewt;
   m.ictl = (int*)(base + L.ictl);
   m.ecache = L.ecache >= 0 ? base + L.ecache : nullptr;
-  m.ncol = L.ncol >= 0 ? base + L.ncol : nullptr;
+  // the CTA's global area: per-warp node scratch (all of it, or the cold parts),
+  // then the new-column buffer when it is not in shared memory
+  double* gbase = nodescr_g ? nodescr_g + (size_t)blockIdx.x * L.gcta : nullptr;
+  const int nw = blockDim.x >> 5;
+  const int gwarp = L.split ? L.nodecold_stride : (L.nodescr_in_smem ? 0 : L.nodescr_stride);
+  m.ncol = L.ncol >= 0 ? base + L.ncol
+                       : ((L.ncol_global && gbase) ? gbase + (size_t)nw * gwarp : nullptr);
+  m.nodecold = (L.split && gbase) ? gbase : nullptr;
+  m.nodecold_stride = L.nodecold_stride;
+  m.ewt_cols = L.ewt_cols;
   m.nrm = base + L.nrm;
   m.ncol_stride = L.ncol_stride;
   m.nodescr_stride = L.nodescr_stride;
-  m.nodescr = L.nodescr_in_smem
-                  ? base + L.nodescr
-                  : nodescr_g + (size_t)blockIdx.x * (blockDim.x >> 5) * L.nodescr_stride;
+  m.nodescr = L.nodescr_in_smem ? base + L.nodescr : gbase;
   return m;
 }
 
@@ -95,7 +107,7 @@ static __device__ __noinline__ double ewald_level0_cached(const DevSys& s, const
   const int np = s.npart, nsec = s.nsec, M = s.nslice, totk = s.totk;
   const int ky0 = s.ikmax[1], kz0 = s.ikmax[2];
   const int nx = s.ikmax[0] + 1, ny = 2 * ky0 + 1;
-  const int w = np + 1;      // the tables area holds w bead columns
+  const int w = m.ewt_cols;  // bead columns of the tables area
   const int chunk = w / 2;   // slices per pass: the old and the new bead of each
   double2* X = (double2*)m.ewt;
   double2* Y = X + nx * w;
@@ -288,16 +300,17 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
                                                    double* ecache, int jcol, bool write,
                                                    double& det, int& err, double* d1,
                                                    double* d2, double* newcol = nullptr,
-                                                   unsigned rowmask = 0xffffffffu) {
+                                                   unsigned rowmask = 0xffffffffu,
+                                                   double* cold = nullptr) {
   if (W == 8)
     node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                       newcol, rowmask);
+                       newcol, rowmask, cold);
   else if (W == 16)
     node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                        newcol, rowmask);
+                        newcol, rowmask, cold);
   else
     node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
-                        newcol, rowmask);
+                        newcol, rowmask, cold);
 }
 
 // Index of the entry's stale-row word (after the element matrices): bit r set
@@ -340,7 +353,6 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
     const int n = s.spec_count[sp];
     const int W = node_group_width(n), g = lane / W;
     const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
-    double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
     const bool mine = sp == msp;
     int start = 0;
     for (int round = 0; round < 64; ++round) {
@@ -367,7 +379,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
       const int nmiss = m.ictl[C_NMISS];
       // warp-wide lane groups when the misses do not fill the warps
       const int Wm = nmiss <= nwarps ? 32 : W, Gm = 32 / Wm, gm = lane / Wm, glm = lane & (Wm - 1);
-      double* scrm = m.nodescr + (size_t)warp * m.nodescr_stride + gm * node_group_scratch(n, !sho);
+      double* scrm = group_scr(m, warp, gm, n, !sho);
+      double* coldm = group_cold(m, warp, gm, n, !sho);
       for (int base = warp * Gm; base < nmiss; base += nwarps * Gm) {
         const int task = base + gm;
         const bool act = task < nmiss;
@@ -385,7 +398,7 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
         double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
         const unsigned rmask = e ? cache_rowmask(e, cache_mask_slot(s, sp)) : 0xffffffffu;
         node_eval_dispatch(Wm, s, sp, v1, v2, sc, scrm, full, ec, -1, act, det, err, d1, d2,
-                           nullptr, rmask);
+                           nullptr, rmask, coldm);
         if (act) {
           if (e && mine && glm < n) {
             e[2 + glm] = d1[glm];
@@ -424,7 +437,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
         int err = errs[k];
         double sc2 = scale[sp];
         int guard = 0;
-        double* dsc = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
+        double* dsc = group_scr(m, warp, g, n, !sho);
+        double* dcold = group_cold(m, warp, g, n, !sho);
         while (err || fabs(det) < 1e-50 || fabs(det) > 1e50) {
           if (err || ++guard > 2000) {
             if (lane == 0) *status |= err ? (PIMC_STATUS_SINGULAR | PIMC_STATUS_RESCALE_LIMIT)
@@ -440,7 +454,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
           double d = 0;
           int e2 = 0;
           node_eval_dispatch(W, s, sp, v1, v2, sc2, dsc, mine ? 1 : 0, nullptr, -1, g == 0, d,
-                             e2, m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm);
+                             e2, m.dist + (k * 2) * nsm, m.dist + (k * 2 + 1) * nsm, nullptr,
+                             0xffffffffu, dcold);
           det = __shfl_sync(0xffffffffu, d, 0);
           err = __shfl_sync(0xffffffffu, e2, 0);
         }
@@ -497,7 +512,8 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
   // (the evaluation is the same, element for element, at any width)
   const int W = ntask <= nwarps ? 32 : node_group_width(n), G = 32 / W, g = lane / W;
   const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
-  double* scr = m.nodescr + (size_t)warp * m.nodescr_stride + g * node_group_scratch(n, !sho);
+  double* scr = group_scr(m, warp, g, n, !sho);
+  double* cold = group_cold(m, warp, g, n, !sho);
   const int jcol = ipart - s.spec_first[msp];
   if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
   __syncthreads();
@@ -516,7 +532,7 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
       ec = m.ecache + (size_t)t * n * n;
     node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
                        m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u);
+                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
     if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);

@@ -28,7 +28,7 @@ struct Smem {
   double* dist;             // [nsec][2][ns_max] distances at set-up (moving species)
   double* ndist;            // [nsec][2][ns_max] distances of the new path
   double* edet;             // [nsec] speculative determinants during set-up
-  double* ewt;              // Ewald exp(ik.r) tables for one slice
+  double* ewt;              // Ewald exp(ik.r) tables: [kx, ky, kz rows][ewt_cols]
   double* qpart;            // [npart] charges
   int* ictl;                // control words
   double* nodescr;          // per-warp node scratch (smem or global)
@@ -37,7 +37,11 @@ struct Smem {
   int ncol_stride;          // ns_max (SHO exp column) or 4 ns_max (free-particle values + gradients)
   double* nrm;              // [2^L - 1][3] the attempt's proposal normals
   int nodescr_stride;       // doubles per warp
+  double* nodecold;         // cold parts of the node scratch when apart (global), or null
+  int nodecold_stride;      // doubles per warp
+  int ewt_cols;             // bead columns of the Ewald tables area
 };
+
 
 enum {
   C_IFIRST1 = 0, C_IFIRST2, C_IPART, C_REJECT, C_FLAG, C_SCANK, C_ERRS, C_NMISS, C_NCTL = 16
@@ -70,6 +74,29 @@ struct SliceView {
 };
 
 // ------------------------------------------------------------------ node model
+// Scratch doubles one lane group needs for an n-particle species: a hot part
+// (the LU and the inverse, rewritten at every elimination step, and the
+// reciprocal pivots) and a cold part (the SHO exp matrix, or the free-particle
+// gradient matrices: written once, read once).
+__host__ __device__ constexpr int node_group_hot(int n) { return 2 * n * n + n + 1; }
+__host__ __device__ constexpr int node_group_cold(int n, bool free_nodes = true) {
+  return n * n + (free_nodes ? 3 * n * n : 0);
+}
+__host__ __device__ constexpr int node_group_scratch(int n, bool free_nodes = true) {
+  return node_group_hot(n) + node_group_cold(n, free_nodes);
+}
+
+// Slater scratch of lane group g of a warp: the hot part (with the cold part
+// after it, unless the layout keeps cold parts apart) and the cold part.
+__device__ __forceinline__ double* group_scr(const Smem& m, int warp, int g, int n, bool free_nodes) {
+  return m.nodescr + (size_t)warp * m.nodescr_stride +
+         g * (m.nodecold ? node_group_hot(n) : node_group_scratch(n, free_nodes));
+}
+__device__ __forceinline__ double* group_cold(const Smem& m, int warp, int g, int n, bool free_nodes) {
+  return m.nodecold ? m.nodecold + (size_t)warp * m.nodecold_stride + g * node_group_cold(n, free_nodes)
+                    : nullptr;
+}
+
 // NodeModel::evaluate (+ evaluateDistance) for one species on one slice pair,
 // executed by a group of W lanes (W = 8, 16 or 32; 32/W groups per warp each
 // take their own slice pair).  Lanes own matrix rows.  LU with partial pivoting
@@ -87,16 +114,18 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
                                 int& err_out, double* d1, double* d2,
-                                double* newcol = nullptr, unsigned rowmask = 0xffffffffu) {
+                                double* newcol = nullptr, unsigned rowmask = 0xffffffffu,
+                                double* cold = nullptr) {
   constexpr unsigned FULL = 0xffffffffu;
   const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
   const int f = s.spec_first[sp];
+  // hot part at scr; the cold part follows it unless given apart
   double* A = scr;          // n*n column-major, LU; after the inverse: the distance weights
   double* X = A + n * n;    // n*n inverse, column-major
-  double* E = X + n * n;    // n*n exp values (SHO nodes)
-  double* R = E + n * n;    // n reciprocals of the U diagonal
-  double* G = R + n + 1;    // 3 n*n gradient factors (free-particle nodes)
+  double* R = X + n * n;    // n reciprocals of the U diagonal
+  double* E = cold ? cold : scr + node_group_hot(n);  // n*n exp values (SHO nodes)
+  double* G = E + n * n;    // 3 n*n gradient factors (free-particle nodes)
   const bool sho = s.node_kind[sp] == 1;
   // --- build the Slater matrix: A(i,j) = scale * rho(r1_j, r2_i)
   // Elements come from ecache where it holds them (a column update keeps every
@@ -404,11 +433,6 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   __syncwarp();
 }
 
-// Scratch doubles one lane group needs for an n-particle species (free-particle
-// nodes keep three gradient matrices besides the LU, inverse and exp matrices).
-__host__ __device__ constexpr int node_group_scratch(int n, bool free_nodes = true) {
-  return 3 * n * n + n + 1 + (free_nodes ? 3 * n * n : 0);
-}
 
 // Group width for an n-particle species.
 __host__ __device__ __forceinline__ int node_group_width(int n) {
@@ -658,10 +682,10 @@ static __device__ void ewald_slice_sums(const DevSys& s, const Smem& m, int ipar
   const int np = s.npart;
   const int kx0 = s.ikmax[0], ky0 = s.ikmax[1], kz0 = s.ikmax[2];
   const int nx = kx0 + 1, ny = 2 * ky0 + 1;
-  double2* X = (double2*)m.ewt;        // [nx][np+1], column np = moved bead
-  double2* Y = X + nx * (np + 1);      // [ny][np+1]
-  double2* Z = Y + ny * (np + 1);      // [nz][np+1]
-  const int w = np + 1;
+  const int w = m.ewt_cols;            // >= np + 1: column np = moved bead
+  double2* X = (double2*)m.ewt;        // [nx][w]
+  double2* Y = X + nx * w;             // [ny][w]
+  double2* Z = Y + ny * w;             // [nz][w]
   __syncthreads();
   for (int p = threadIdx.x; p < w; p += blockDim.x) {
     if (p < np)

@@ -292,6 +292,26 @@ def test_launch_configs_match_golden(pimc, case, block, scratch_global, regs):
     assert rel_close(rec["ds_node"][0][:, :nl], ref["ds_node"][:n, :nl], NODE_TOL.get(case, 1e-10))
 
 
+@pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 2), (128, 0, 2), (256, 0, 2),
+                                                       (512, 0, 1), (256, 1, 2)])
+def test_electron_gas_scratch_placements(pimc, block, scratch_global, regs):
+    # 27 x 27 free-particle matrices: every shared-memory placement of the Slater
+    # scratch (whole, hot part with the cold part and the new-column buffer in
+    # global memory, all in global memory) reproduces pi-qmc's records.
+    g = golden_io.load("heg54")
+    e = engine_for(pimc, g)
+    e.configure(block, scratch_global, 0, regs)
+    e.upload_paths([g["path0"]])
+    rec = e.run_sections(g["nattempt"], records=True)
+    ref = g["records"]
+    for k in ("ifirst1", "ipart", "reject_level"):
+        assert np.array_equal(rec[k][0], ref[k]), k
+    nl = g["kw"]["nlevel"] + 1
+    assert rel_close(rec["ds"][0][:, :nl], ref["ds"][:, :nl], 1e-12)
+    assert rel_close(rec["ds_node"][0][:, :nl], ref["ds_node"][:, :nl], 1e-10)
+    assert np.abs(e.download_paths()[0] - g["path1"]).max() <= 1e-12
+
+
 def test_autotune_does_not_advance_chains(pimc):
     g = golden_io.load("dot4_fn")
     a = engine_for(pimc, g, nreplica=8)
