@@ -106,11 +106,11 @@ def sweep_attempts(kw):
 # profiles/fp64_work_per_attempt.md; they are the roofline numerator.
 MEASURED_WORK = {
     # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
-    ("dot20_fn", "mixed"): (2.654e5, 8.201e4),
-    ("dot20_fn", "fp64"): (4.872e5, 8.206e4),
-    ("batch4096", "mixed"): (2.334e5, 3.26e4),   # counted on the first 1024 replicas
-    ("heg54", "mixed"): (4.507e6, 1.914e6),     # with the structure-factor cache
-    ("dot2", "fp64"): (1.933e4, 459.6),
+    ("dot20_fn", "mixed"): (2.654e5, 8.204e4),
+    ("dot20_fn", "fp64"): (4.873e5, 8.198e4),
+    ("batch4096", "mixed"): (1.783e5, 3.075e4),   # counted on the first 1024 replicas
+    ("heg54", "mixed"): (4.507e6, 1.752e6),
+    ("dot2", "fp64"): (1.933e4, 524.0),
 }
 
 
