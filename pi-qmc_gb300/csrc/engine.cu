@@ -381,7 +381,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.dist = take(fixed ? nsec * 2 * nsm : 0);
   L.ndist = take(fixed ? nsec * 2 * nsm : 0);
   L.ewt = take(2 * per * L.ewt_cols);
-  L.ictl = take((C_NCTL + 2 * nsec + 1) / 2 + 1);
+  L.ictl = take((C_NCTL + 2 * kMaxSpecies * nsec + 1) / 2 + 1);
   bool sho = false;
   for (const DevSys& d : sys)
     for (int i = 0; i < d.nspecies; ++i) sho |= d.node_kind[i] == PIMC_NODES_SHO;

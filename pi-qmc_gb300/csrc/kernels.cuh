@@ -335,92 +335,129 @@ __device__ __forceinline__ double* cache_entry(const DevSys& s, double* cache, i
   return cache + ((size_t)sp * s.nslice + t1) * s.nc_stride;
 }
 
+// One pass of the set-up over slices [start, nsec) of one node species (only_sp)
+// or of all of them (only_sp < 0): cached results are copied, the others are
+// evaluated, the species' warps side by side.  Determinants go to dm[sp][t],
+// error flags to errs[sp][t], the moving species' distances to dist.
+static __device__ void node_init_pass(const DevSys& s, const Smem& m, const double* scale,
+                                      const int* epoch, int msp, double* cache, int ifirst1,
+                                      int only_sp, int start) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int nsec = s.nsec, M = s.nslice, nsm = s.ns_max;
+  int* errs = m.ictl + C_NCTL;                 // [kMaxSpecies][nsec]
+  int* miss = errs + kMaxSpecies * nsec;       // [kMaxSpecies][nsec] slices to evaluate
+  int* nmiss = m.ictl + C_NMISS;               // [kMaxSpecies] (C_NMISS .. C_NMISS + 3)
+  const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+  if (threadIdx.x < kMaxSpecies) nmiss[threadIdx.x] = 0;
+  __syncthreads();
+  const int nt = nsec - start;
+  for (int it = threadIdx.x; it < s.nspecies * nt; it += blockDim.x) {
+    const int sp = it / nt, t = start + (it - sp * nt);
+    if (!s.node_kind[sp] || (only_sp >= 0 && sp != only_sp)) continue;
+    const int n = s.spec_count[sp];
+    const double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
+    if (e && e[0] == (double)epoch[sp]) {
+      m.dm[sp * nsec + t] = e[1];
+      errs[sp * nsec + t] = 0;
+      if (sp == msp)
+        for (int j = 0; j < n; ++j) {
+          m.dist[(t * 2) * nsm + j] = e[2 + j];
+          m.dist[(t * 2 + 1) * nsm + j] = e[2 + n + j];
+        }
+    } else {
+      miss[sp * nsec + atomicAdd(&nmiss[sp], 1)] = t;
+    }
+  }
+  __syncthreads();
+  // warp tasks: each warp takes up to G misses of one species (lane groups of
+  // a warp must run the same species so that they stay converged); lane
+  // groups as wide as the warp when the misses do not fill the warps
+  int total = 0, ntask = 0;
+  for (int sp = 0; sp < s.nspecies; ++sp) total += nmiss[sp];
+  int Gs[kMaxSpecies], Ws[kMaxSpecies], first[kMaxSpecies + 1];
+  for (int sp = 0; sp < s.nspecies; ++sp) {
+    Ws[sp] = total <= nwarps ? 32 : node_group_width(s.spec_count[sp]);
+    Gs[sp] = 32 / Ws[sp];
+    first[sp] = ntask;
+    ntask += (nmiss[sp] + Gs[sp] - 1) / Gs[sp];
+  }
+  first[s.nspecies] = ntask;
+  for (int wt = warp; wt < ntask; wt += nwarps) {
+    int sp = 0;
+    while (wt >= first[sp + 1]) ++sp;
+    const int n = s.spec_count[sp];
+    const bool sho = s.node_kind[sp] == PIMC_NODES_SHO, mine = sp == msp;
+    const int W = Ws[sp], gm = lane / W, glm = lane & (W - 1);
+    const int base = (wt - first[sp]) * Gs[sp];
+    const int task = base + gm;
+    const bool act = task < nmiss[sp];
+    const int t = miss[sp * nsec + (act ? task : base)];
+    double* scrm = group_scr(m, warp, gm, n, !sho);
+    double* coldm = group_cold(m, warp, gm, n, !sho);
+    double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
+    SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
+    SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
+    double det = 0;
+    int err = 0;
+    double* ec = e ? e + 2 + 2 * n
+                   : ((sho && mine && m.ecache) ? m.ecache + (size_t)t * n * n : nullptr);
+    // with a cache every miss is evaluated in full so that its entry is complete
+    const int full = (mine || e) ? 1 : 0;
+    double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
+    double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
+    const unsigned rmask = e ? cache_rowmask(e, cache_mask_slot(s, sp)) : 0xffffffffu;
+    node_eval_dispatch(W, s, sp, v1, v2, scale[sp], scrm, full, ec, -1, act, det, err, d1, d2,
+                       nullptr, rmask, coldm);
+    if (act) {
+      if (e && mine && glm < n) {
+        e[2 + glm] = d1[glm];
+        e[2 + n + glm] = d2[glm];
+      }
+      if (glm == 0) {
+        m.dm[sp * nsec + t] = det;
+        errs[sp * nsec + t] = err;
+        if (e) {
+          e[1] = det;
+          e[0] = err ? NaN : (double)epoch[sp];
+          e[cache_mask_slot(s, sp)] = 0.0;  // the element matrix is whole again
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // FixedNodeAction::initialize (src/fixednode/FixedNodeAction.cc:331-357) for every
 // species with a node model, reproducing NodeModel::evaluate's rescaling loop
-// (src/fixednode/SHONodes.cc:112-126): slices are evaluated in parallel at the
-// current scale; at the first slice whose determinant leaves [1e-50, 1e50] the
-// loop is replayed sequentially, and later slices are re-evaluated.
+// (src/fixednode/SHONodes.cc:112-126): every species' slices are evaluated in
+// parallel at the current scales (pi-qmc sets the species up one after the
+// other; they are independent); at a species' first slice whose determinant
+// leaves [1e-50, 1e50] its loop is replayed sequentially, and its later
+// slices are re-evaluated.
 static __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
                                 int msp, uint32_t* status, double* cache, int ifirst1) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nsec = s.nsec, M = s.nslice;
   const int nsm = s.ns_max;
-  int* errs = m.ictl + C_NCTL;          // [nsec]
-  int* miss = m.ictl + C_NCTL + nsec;   // [nsec]
+  int* errs = m.ictl + C_NCTL;  // [kMaxSpecies][nsec]
   const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+  node_init_pass(s, m, scale, epoch, msp, cache, ifirst1, -1, 0);
   for (int sp = 0; sp < s.nspecies; ++sp) {
     if (!s.node_kind[sp]) continue;
     const int n = s.spec_count[sp];
     const int W = node_group_width(n), g = lane / W;
     const bool sho = s.node_kind[sp] == PIMC_NODES_SHO;
     const bool mine = sp == msp;
+    double* dm = m.dm + sp * nsec;
+    int* er = errs + sp * nsec;
     int start = 0;
     for (int round = 0; round < 64; ++round) {
-      const double sc = scale[sp];
-      const double ep = (double)epoch[sp];
-      // hits: copy cached results; misses: list them
-      if (threadIdx.x == 0) m.ictl[C_NMISS] = 0;
-      __syncthreads();
-      for (int t = start + (int)threadIdx.x; t < nsec; t += blockDim.x) {
-        const double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
-        if (e && e[0] == ep) {
-          m.edet[t] = e[1];
-          errs[t] = 0;
-          if (mine)
-            for (int j = 0; j < n; ++j) {
-              m.dist[(t * 2) * nsm + j] = e[2 + j];
-              m.dist[(t * 2 + 1) * nsm + j] = e[2 + n + j];
-            }
-        } else {
-          miss[atomicAdd(&m.ictl[C_NMISS], 1)] = t;
-        }
-      }
-      __syncthreads();
-      const int nmiss = m.ictl[C_NMISS];
-      // warp-wide lane groups when the misses do not fill the warps
-      const int Wm = nmiss <= nwarps ? 32 : W, Gm = 32 / Wm, gm = lane / Wm, glm = lane & (Wm - 1);
-      double* scrm = group_scr(m, warp, gm, n, !sho);
-      double* coldm = group_cold(m, warp, gm, n, !sho);
-      for (int base = warp * Gm; base < nmiss; base += nwarps * Gm) {
-        const int task = base + gm;
-        const bool act = task < nmiss;
-        const int t = miss[act ? task : base];
-        double* e = cache ? cache_entry(s, cache, sp, wrap_slice(ifirst1 + t, M)) : nullptr;
-        SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, -1, 0, 0, 0};
-        SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
-        double det = 0;
-        int err = 0;
-        double* ec = e ? e + 2 + 2 * n
-                       : ((sho && mine && m.ecache) ? m.ecache + (size_t)t * n * n : nullptr);
-        // with a cache every miss is evaluated in full so that its entry is complete
-        const int full = (mine || e) ? 1 : 0;
-        double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
-        double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
-        const unsigned rmask = e ? cache_rowmask(e, cache_mask_slot(s, sp)) : 0xffffffffu;
-        node_eval_dispatch(Wm, s, sp, v1, v2, sc, scrm, full, ec, -1, act, det, err, d1, d2,
-                           nullptr, rmask, coldm);
-        if (act) {
-          if (e && mine && glm < n) {
-            e[2 + glm] = d1[glm];
-            e[2 + n + glm] = d2[glm];
-          }
-          if (glm == 0) {
-            m.edet[t] = det;
-            errs[t] = err;
-            if (e) {
-              e[1] = det;
-              e[0] = err ? NaN : ep;
-              e[cache_mask_slot(s, sp)] = 0.0;  // the element matrix is whole again
-            }
-          }
-        }
-      }
-      __syncthreads();
+      if (round > 0) node_init_pass(s, m, scale, epoch, msp, cache, ifirst1, sp, start);
       if (threadIdx.x == 0) {
         int k = -1;
         for (int t = start; t < nsec; ++t) {
-          const double a = fabs(m.edet[t]);
-          if (errs[t] || a < 1e-50 || a > 1e50) {
+          const double a = fabs(dm[t]);
+          if (er[t] || a < 1e-50 || a > 1e50) {
             k = t;
             break;
           }
@@ -433,8 +470,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
       if (warp == 0) {
         // pi-qmc's do-while rescale loop on slice k, by group 0 of warp 0
         // (the other groups repeat it without storing).
-        double det = m.edet[k];
-        int err = errs[k];
+        double det = dm[k];
+        int err = er[k];
         double sc2 = scale[sp];
         int guard = 0;
         double* dsc = group_scr(m, warp, g, n, !sho);
@@ -460,8 +497,8 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
           err = __shfl_sync(0xffffffffu, e2, 0);
         }
         if (lane == 0) {
-          m.edet[k] = det;
-          errs[k] = err;
+          dm[k] = det;
+          er[k] = err;
           if (sc2 != scale[sp]) epoch[sp] += 1;
           scale[sp] = sc2;
           if (cache) cache_entry(s, cache, sp, wrap_slice(ifirst1 + k, M))[0] = NaN;
@@ -473,12 +510,9 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
     }
     // crossing check, as the reference counts errors at set-up
     if (threadIdx.x == 0) {
-      for (int t = 0; t < nsec; ++t) {
-        m.dm[sp * nsec + t] = m.edet[t];
-        if (errs[t] || m.edet[t] * m.edet[0] <= 1e-200) *status |= PIMC_STATUS_INIT_CROSSING;
-      }
+      for (int t = 0; t < nsec; ++t)
+        if (er[t] || dm[t] * dm[0] <= 1e-200) *status |= PIMC_STATUS_INIT_CROSSING;
     }
-    __syncthreads();
   }
   if (msp >= 0 && s.node_kind[msp]) {
     // newDist(0) = dist(0)
