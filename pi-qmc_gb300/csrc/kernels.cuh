@@ -599,6 +599,71 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
   return block_sum(part, m.red);
 }
 
+// node_level for levels lo .. hi (all above 0) at once: the changed slices of
+// every level in the range are evaluated side by side (a level's proposal does
+// not depend on the decisions above it), and dsn[l] gets level l's difference
+// (2e100 when a changed slice of that level crosses a node, else 0).  The
+// caller applies pi-qmc's level-by-level decisions to the results.
+static __device__ void node_level_range(const DevSys& s, const Smem& m, double scale, int msp,
+                                        int ipart, int lo, int hi, double* cache, int ifirst1,
+                                        double* dsn) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
+  const int n = s.spec_count[msp];
+  if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
+  __syncthreads();
+  if (hi == L) {
+    // the top level's only slice is the section's fixed end: copied from the set-up
+    const int t = nsec - 1;
+    for (int i = threadIdx.x; i < 2 * nsm; i += blockDim.x) m.ndist[t * 2 * nsm + i] = m.dist[t * 2 * nsm + i];
+    if (threadIdx.x == 0) {
+      m.ndm[t] = m.dm[msp * nsec + t];
+      if (m.ndm[t] * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << L);
+    }
+  }
+  // tasks: level l's slices 2^l (2k + 1), levels hi' .. lo (hi' = hi, or L - 1)
+  const int top = hi == L ? L - 1 : hi;
+  int ntask = 0;
+  for (int l = top; l >= lo; --l) ntask += (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
+  const int W = ntask <= nwarps ? 32 : node_group_width(n), G = 32 / W, g = lane / W;
+  const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
+  double* scr = group_scr(m, warp, g, n, !sho);
+  double* cold = group_cold(m, warp, g, n, !sho);
+  const int jcol = ipart - s.spec_first[msp];
+  for (int base = warp * G; base < ntask; base += nwarps * G) {
+    const int task = base + g;
+    const bool act = task < ntask;
+    // task -> (level, slice)
+    int k = act ? task : base, l = top;
+    for (;;) {
+      const int nl = (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
+      if (k < nl || l == lo) break;
+      k -= nl;
+      --l;
+    }
+    const int t = (1 << l) + k * (1 << (l + 1));
+    SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
+    SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
+    double det = 0;
+    int err = 0;
+    double* ec = nullptr;
+    if (cache)
+      ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
+    else if (sho && m.ecache)
+      ec = m.ecache + (size_t)t * n * n;
+    node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
+                       m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
+                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
+    if (act && (lane & (W - 1)) == 0) {
+      m.ndm[t] = det;
+      if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << l);
+    }
+  }
+  __syncthreads();
+  const int flags = m.ictl[C_FLAG];
+  for (int l = lo; l <= hi; ++l) dsn[l] = ((flags >> l) & 1) ? 2e100 : 0.0;
+}
+
 // The uniform-stream index of the first uniform consumed at `level`
 // (image choices of FreeMoverPBC, then the Metropolis uniform).
 __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int level) {
@@ -703,7 +768,56 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       pimc_move_record* rec = P.rec ? P.rec + (size_t)r * P.nattempt + a : nullptr;
       double oldDS = 0.0;
       int reject = -1;
-      for (int level = L; level >= 0; --level) {
+      // The top levels (L down to lb) are proposed and evaluated together,
+      // their Slater matrices side by side; the decisions then follow level by
+      // level exactly as below.  Work done for levels under a rejection is
+      // discarded.
+      const int lb = L >= 2 ? max(1, L - 3) : L + 1;
+      if (lb <= L) {
+        double* lds = m.red + kWarps + 8;  // [kMaxLevels] per level: action difference,
+        double* llt = lds + kMaxLevels;     // mover ln T,
+        double* lnd = llt + kMaxLevels;     // fixed-node difference
+        for (int level = L; level >= lb; --level) {
+          const uint32_t ubase = level_uniform_base(s, level);
+          const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
+          const double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
+          if (threadIdx.x == 0) {
+            lds[level] = ds;
+            llt[level] = lnT;
+            lnd[level] = 0.0;
+          }
+        }
+        if (mynode) node_level_range(s, m, scale[msp], msp, ipart, lb, L, cache, ifirst1, lnd);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double old = 0.0;
+          for (int level = L; level >= lb; --level) {
+            const double ds = lds[level], dsn = lnd[level], lnT = llt[level];
+            const double total = s.fixed_node ? ds + dsn : ds;
+            const uint32_t ubase = level_uniform_base(s, level);
+            const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
+            const uint32_t uacc = ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
+            const double p = exp(lnT + (-total + old));
+            const double u = stream_uniform(P.seed, s.stream_id, att, uacc);
+            if (rec) {
+              rec->ds[level] = ds;
+              rec->ds_node[level] = dsn;
+              rec->lnt[level] = lnT;
+            }
+            if (!(isfinite(lnT) && isfinite(ds))) status |= PIMC_STATUS_NONFINITE;
+            old = total;
+            if (u > p) {
+              m.ictl[C_REJECT] = level;
+              break;
+            }
+          }
+          m.red[kWarps + 2] = old;
+        }
+        __syncthreads();
+        reject = m.ictl[C_REJECT];
+        oldDS = m.red[kWarps + 2];
+      }
+      for (int level = min(L, lb - 1); level >= 0 && reject < 0; --level) {
         const uint32_t ubase = level_uniform_base(s, level);
         const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
         double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
