@@ -370,13 +370,12 @@ static __device__ void node_init_pass(const DevSys& s, const Smem& m, const doub
   }
   __syncthreads();
   // warp tasks: each warp takes up to G misses of one species (lane groups of
-  // a warp must run the same species so that they stay converged); lane
-  // groups as wide as the warp when the misses do not fill the warps
+  // a warp must run the same species so that they stay converged)
   int total = 0, ntask = 0;
   for (int sp = 0; sp < s.nspecies; ++sp) total += nmiss[sp];
   int Gs[kMaxSpecies], Ws[kMaxSpecies], first[kMaxSpecies + 1];
   for (int sp = 0; sp < s.nspecies; ++sp) {
-    Ws[sp] = total <= nwarps ? 32 : node_group_width(s.spec_count[sp]);
+    Ws[sp] = node_group_width(s.spec_count[sp]);
     Gs[sp] = 32 / Ws[sp];
     first[sp] = ntask;
     ntask += (nmiss[sp] + Gs[sp] - 1) / Gs[sp];
@@ -542,9 +541,10 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
     __syncthreads();
     return m.ictl[C_FLAG] ? 2e100 : 0.0;
   }
-  // lane groups as wide as the warp when the tasks do not fill the warps
-  // (the evaluation is the same, element for element, at any width)
-  const int W = ntask <= nwarps ? 32 : node_group_width(n), G = 32 / W, g = lane / W;
+  // lane groups of the species' width, packed (32 / W matrices a warp): the
+  // SM's narrow FP64 pipe, shared by every resident warp, is the limit, and a
+  // packed warp instruction serves several matrices
+  const int W = node_group_width(n), G = 32 / W, g = lane / W;
   const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
   double* scr = group_scr(m, warp, g, n, !sho);
   double* cold = group_cold(m, warp, g, n, !sho);
@@ -625,7 +625,7 @@ static __device__ void node_level_range(const DevSys& s, const Smem& m, double s
   const int top = hi == L ? L - 1 : hi;
   int ntask = 0;
   for (int l = top; l >= lo; --l) ntask += (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
-  const int W = ntask <= nwarps ? 32 : node_group_width(n), G = 32 / W, g = lane / W;
+  const int W = node_group_width(n), G = 32 / W, g = lane / W;
   const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
   double* scr = group_scr(m, warp, g, n, !sho);
   double* cold = group_cold(m, warp, g, n, !sho);

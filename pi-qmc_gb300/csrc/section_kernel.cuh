@@ -246,7 +246,7 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
         }
       }
       __syncwarp();
-      const double rinv = 1.0 / A[j * n + j];
+      const double rinv = __drcp_rn(A[j * n + j]);  // 1 / a, correctly rounded
       if (gl == j) R[j] = rinv;
       if (gl > j && gl < n) A[j * n + gl] *= rinv;
     } else if (info == 0) {
@@ -275,7 +275,8 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   double det = 1.0;
   for (int i = 0; i < n; ++i) {
     det *= A[i * n + i];
-    det *= ((pivbits >> i) & 1u) ? -1 : 1;
+    // times -1 for an interchanged row: a sign flip, exactly that product
+    if ((pivbits >> i) & 1u) det = __longlong_as_double(__double_as_longlong(det) ^ (1LL << 63));
   }
   if (write) {
     det_out = det;
