@@ -360,42 +360,42 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
     __syncwarp();
     const double c = s.node_c[sp], ch = s.node_cosh[sp];
     const double fac = 2 * c * scale;
+    // sum_i w(i,j) (r2_i - ch r1_j) = S - ch r1_j T with S = sum_i w(i,j) r2_i and
+    // T = sum_i w(i,j): four FP64 operations a term instead of six
     if (ok && gl < n) {
       const int j = gl;  // d1: sum_i w(i,j) 2c (r2_i - ch r1_j)
       double rjx, rjy, rjz;
       v1.get(f + j, rjx, rjy, rjz);
-      const double cx = ch * rjx, cy = ch * rjy, cz = ch * rjz;
-      double lx = 0, ly = 0, lz = 0;
+      double sx = 0, sy = 0, sz = 0, tw = 0;
       for (int i = 0; i < n; ++i) {
         double rix, riy, riz;
         v2.get(f + i, rix, riy, riz);
         const double w = A[j * n + i];
-        lx += w * (rix - cx);
-        ly += w * (riy - cy);
-        lz += w * (riz - cz);
+        sx += w * rix;
+        sy += w * riy;
+        sz += w * riz;
+        tw += w;
       }
-      lx *= fac;
-      ly *= fac;
-      lz *= fac;
+      const double ct = ch * tw;
+      const double lx = fac * (sx - ct * rjx), ly = fac * (sy - ct * rjy), lz = fac * (sz - ct * rjz);
       if (write) d1[j] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
     }
     if (ok && gl < n) {
       const int i = gl;  // d2: sum_j w(i,j) 2c (r1_j - ch r2_i)
       double rix, riy, riz;
       v2.get(f + i, rix, riy, riz);
-      const double cx = ch * rix, cy = ch * riy, cz = ch * riz;
-      double lx = 0, ly = 0, lz = 0;
+      double sx = 0, sy = 0, sz = 0, tw = 0;
       for (int j = 0; j < n; ++j) {
         double rjx, rjy, rjz;
         v1.get(f + j, rjx, rjy, rjz);
         const double w = A[j * n + i];
-        lx += w * (rjx - cx);
-        ly += w * (rjy - cy);
-        lz += w * (rjz - cz);
+        sx += w * rjx;
+        sy += w * rjy;
+        sz += w * rjz;
+        tw += w;
       }
-      lx *= fac;
-      ly *= fac;
-      lz *= fac;
+      const double ct = ch * tw;
+      const double lx = fac * (sx - ct * rix), ly = fac * (sy - ct * riy), lz = fac * (sz - ct * riz);
       if (write) d2[i] = dk * rsqrt(dot3(lx, ly, lz, lx, ly, lz) + 1e-15);
     }
   } else {
