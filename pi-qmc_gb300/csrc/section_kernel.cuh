@@ -236,7 +236,7 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
     const int p = __shfl_sync(FULL, ai, 0, W);
     if (gl == j) piv_lane = p;
     const double apj = A[j * n + p];
-    if (apj != 0.0) {
+    if (__double_as_longlong(apj) & 0x7fffffffffffffffLL) {  // apj != 0, on the integer pipe
       if (p != j) {
         pivbits |= 1u << j;
         for (int k = gl; k < n; k += W) {
@@ -294,26 +294,26 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   }
   // Column c of X starts as e_pos(c); the substitutions then run one element
   // (column, row) per lane and step.  Every element receives the same FMAs in
-  // the same order as a per-column solve (the steps before pos(c) subtract
-  // exact zeros), so the result is that solve's, bit for bit.
+  // the same order as a per-column solve, so the result is that solve's, bit
+  // for bit: the forward steps before pos(c) would only subtract exact zeros
+  // from zeros, and are skipped.
   const bool inv_ok = info == 0;
   if (inv_ok && gl < n)
     for (int i = 0; i < n; ++i) X[gl * n + i] = (i == pos) ? 1.0 : 0.0;
+  int ordc = 0;  // the column whose unit vector sits at row gl
+  for (int c = 0; c < n; ++c)
+    if (__shfl_sync(FULL, pos, c, W) == gl) ordc = c;
   __syncwarp();
   for (int j = 0; j < n - 1; ++j) {  // forward: x(i) -= l(i,j) x(j), i > j
-    const int m = n - j - 1;
-    if (inv_ok) {
-      int c = gl / m, ii = gl - c * m;
-      const int dc = W / m, di = W - dc * m;
-      for (int e = gl; e < n * m; e += W) {
-        const int i = j + 1 + ii;
+    // the columns nonzero at row j: order[q] for q <= j, rows j+1 .. n-1
+    const int m = n - j - 1, cnt = (j + 1) * m;
+    for (int e0 = 0; e0 < cnt; e0 += W) {
+      const int e = e0 + gl;
+      const int q = e < cnt ? e / m : 0;
+      const int c = __shfl_sync(FULL, ordc, q, W);
+      if (inv_ok && e < cnt) {
+        const int i = j + 1 + (e - q * m);
         X[c * n + i] -= A[j * n + i] * X[c * n + j];
-        ii += di;
-        c += dc;
-        if (ii >= m) {
-          ii -= m;
-          ++c;
-        }
       }
     }
     __syncwarp();
