@@ -374,6 +374,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.mv = take(3 * nsec);
   L.nrm = take(3 * nsec);
   L.red = take(64);
+  L.vred = take(9 * kWarps);
   L.q = take(np);
   L.dm = take(kMaxSpecies * nsec);
   L.ndm = take(nsec);
@@ -481,6 +482,7 @@ Layout estimator_layout(const std::vector<DevSys>& sys, const int* ikmax_extra) 
   L.mv = take(3 * nsec);
   L.nrm = L.mv;
   L.red = take(64);
+  L.vred = L.red;
   L.q = take(np);
   L.ewt = take(2 * ((ik[0] + 1) + (2 * ik[1] + 1) + (2 * ik[2] + 1)) * (np + 1));
   L.ictl = take(C_NCTL + 2);

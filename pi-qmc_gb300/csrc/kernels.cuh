@@ -12,6 +12,7 @@ struct Layout {
   int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
   int ncol_stride;
   int nrm;  // the attempt's normals, 3 per movable slice
+  int vred;             // vector reductions: [8][kWarps] partials, then 8 sums
   int nodescr_in_smem;  // the node scratch (its hot parts when split) in shared memory
   int nodescr_stride;   // doubles per warp of that scratch
   int split;            // cold parts apart, in the CTA's global area
@@ -55,6 +56,7 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.my = m.mx + s.nsec;
   m.mz = m.my + s.nsec;
   m.red = base + L.red;
+  m.vred = base + L.vred;
   m.qpart = base + L.q;
   m.dm = base + L.dm;
   m.ndm = base + L.ndm;
@@ -204,7 +206,7 @@ static __device__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t 
   }
 }
 
-static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
+static __device__ double mover_level_part(const DevSys& s, const Smem& m, int ipart, int level,
                               uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
@@ -290,7 +292,31 @@ static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, 
     }
     part += acc;
   }
-  return block_sum(part, m.red);
+  return part;
+}
+
+// FreeMover(PBC)::makeMove for one level: the beads, and ln(T_old/T_new) summed over the block.
+static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
+                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
+  return block_sum(mover_level_part(s, m, ipart, level, seed, rep, att, ubase), m.red);
+}
+
+// Block sums of nv per-thread values (nv <= 8) in a fixed order: warp trees,
+// then the warps in turn; out[v] is visible to every thread on return.
+__device__ __forceinline__ void block_sum_vec(const double* v, int nv, double* buf, double* out) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = 0; k < nv; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (l == 0) buf[k * kWarps + w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double x = 0.0;
+    for (int i = 0; i < nw; ++i) x += buf[threadIdx.x * kWarps + i];
+    out[threadIdx.x] = x;
+  }
+  __syncthreads();
 }
 
 // Evaluates one slice pair per lane group (group width W from the species size).
@@ -599,71 +625,6 @@ static __device__ double node_level(const DevSys& s, const Smem& m, double scale
   return block_sum(part, m.red);
 }
 
-// node_level for levels lo .. hi (all above 0) at once: the changed slices of
-// every level in the range are evaluated side by side (a level's proposal does
-// not depend on the decisions above it), and dsn[l] gets level l's difference
-// (2e100 when a changed slice of that level crosses a node, else 0).  The
-// caller applies pi-qmc's level-by-level decisions to the results.
-static __device__ void node_level_range(const DevSys& s, const Smem& m, double scale, int msp,
-                                        int ipart, int lo, int hi, double* cache, int ifirst1,
-                                        double* dsn) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
-  const int n = s.spec_count[msp];
-  if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
-  __syncthreads();
-  if (hi == L) {
-    // the top level's only slice is the section's fixed end: copied from the set-up
-    const int t = nsec - 1;
-    for (int i = threadIdx.x; i < 2 * nsm; i += blockDim.x) m.ndist[t * 2 * nsm + i] = m.dist[t * 2 * nsm + i];
-    if (threadIdx.x == 0) {
-      m.ndm[t] = m.dm[msp * nsec + t];
-      if (m.ndm[t] * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << L);
-    }
-  }
-  // tasks: level l's slices 2^l (2k + 1), levels hi' .. lo (hi' = hi, or L - 1)
-  const int top = hi == L ? L - 1 : hi;
-  int ntask = 0;
-  for (int l = top; l >= lo; --l) ntask += (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
-  const int W = node_group_width(n), G = 32 / W, g = lane / W;
-  const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
-  double* scr = group_scr(m, warp, g, n, !sho);
-  double* cold = group_cold(m, warp, g, n, !sho);
-  const int jcol = ipart - s.spec_first[msp];
-  for (int base = warp * G; base < ntask; base += nwarps * G) {
-    const int task = base + g;
-    const bool act = task < ntask;
-    // task -> (level, slice)
-    int k = act ? task : base, l = top;
-    for (;;) {
-      const int nl = (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
-      if (k < nl || l == lo) break;
-      k -= nl;
-      --l;
-    }
-    const int t = (1 << l) + k * (1 << (l + 1));
-    SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
-    SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
-    double det = 0;
-    int err = 0;
-    double* ec = nullptr;
-    if (cache)
-      ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
-    else if (sho && m.ecache)
-      ec = m.ecache + (size_t)t * n * n;
-    node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
-                       m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
-    if (act && (lane & (W - 1)) == 0) {
-      m.ndm[t] = det;
-      if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << l);
-    }
-  }
-  __syncthreads();
-  const int flags = m.ictl[C_FLAG];
-  for (int l = lo; l <= hi; ++l) dsn[l] = ((flags >> l) & 1) ? 2e100 : 0.0;
-}
-
 // The uniform-stream index of the first uniform consumed at `level`
 // (image choices of FreeMoverPBC, then the Metropolis uniform).
 __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int level) {
@@ -675,6 +636,108 @@ __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int leve
   }
   return u;
 }
+
+// The top bisection levels lo .. hi (all above 0) at once: the movers, level
+// by level (a level's midpoints are the beads of the levels above), then the
+// changed slices of every level in the range on the first warps, side by side,
+// while the remaining warps compute the levels' action differences (a level's
+// proposal does not depend on the decisions above it).  Per level l: lds[l]
+// the action difference, llt[l] the mover's ln(T_old/T_new), lnd[l] the
+// fixed-node difference (2e100 when a changed slice crosses a node, else 0).
+// The caller applies pi-qmc's level-by-level decisions to them.
+static __device__ void top_levels(const DevSys& s, const Smem& m, double scale, int msp,
+                                  int ipart, int lo, int hi, bool mynode, double* cache,
+                                  int ifirst1, uint64_t seed, uint32_t att, double* lds,
+                                  double* llt, double* lnd) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
+  const int nb = hi - lo + 1;  // <= 4
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // [0, nb): mover terms, [4, 4 + nb): action terms
+  for (int level = hi; level >= lo; --level) {
+    const double p = mover_level_part(s, m, ipart, level, seed, s.stream_id, att,
+                                      level_uniform_base(s, level));
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k == hi - level) v[k] = p;
+    __syncthreads();  // this level's beads before the next level's midpoints
+  }
+  const int n = mynode ? s.spec_count[msp] : 1;
+  const int top = hi == L ? L - 1 : hi;
+  int ntask = 0;
+  if (mynode)
+    for (int l = top; l >= lo; --l) ntask += (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
+  const int W = node_group_width(n), G = 32 / W, g = lane / W;
+  const int nodeW = min(nwarps, (ntask + G - 1) / G);
+  if (threadIdx.x == 0) m.ictl[C_FLAG] = 0;
+  if (mynode && hi == L) {
+    // the top level's only slice is the section's fixed end: copied from the set-up
+    const int t = nsec - 1;
+    for (int i = threadIdx.x; i < 2 * nsm; i += blockDim.x) m.ndist[t * 2 * nsm + i] = m.dist[t * 2 * nsm + i];
+  }
+  __syncthreads();
+  if (mynode && hi == L && threadIdx.x == 0) {
+    const int t = nsec - 1;
+    m.ndm[t] = m.dm[msp * nsec + t];
+    if (m.ndm[t] * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << L);
+  }
+  if (warp < nodeW) {
+    const bool sho = s.node_kind[msp] == PIMC_NODES_SHO;
+    double* scr = group_scr(m, warp, g, n, !sho);
+    double* cold = group_cold(m, warp, g, n, !sho);
+    const int jcol = ipart - s.spec_first[msp];
+    for (int base = warp * G; base < ntask; base += nodeW * G) {
+      const int task = base + g;
+      const bool act = task < ntask;
+      int k = act ? task : base, l = top;  // task -> (level, slice)
+      for (;;) {
+        const int nl = (nsec - 1 - (1 << l)) / (1 << (l + 1)) + 1;
+        if (k < nl || l == lo) break;
+        k -= nl;
+        --l;
+      }
+      const int t = (1 << l) + k * (1 << (l + 1));
+      SliceView v1{m.s1x, m.s1y, m.s1z, s.npart, t, ipart, m.mx[t], m.my[t], m.mz[t]};
+      SliceView v2{m.s2x, m.s2y, m.s2z, s.npart, t, -1, 0, 0, 0};
+      double det = 0;
+      int err = 0;
+      double* ec = nullptr;
+      if (cache)
+        ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
+      else if (sho && m.ecache)
+        ec = m.ecache + (size_t)t * n * n;
+      node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
+                         m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
+                         cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
+      if (act && (lane & (W - 1)) == 0) {
+        m.ndm[t] = det;
+        if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << l);
+      }
+    }
+  }
+  // the action differences on the other warps (on all of them when the node
+  // tasks take every warp, after those)
+  if (nodeW == nwarps) __syncthreads();
+  const int a0 = nodeW == nwarps ? 0 : nodeW * 32;
+  if ((int)threadIdx.x >= a0)
+    for (int level = lo; level <= hi; ++level) {
+      const double a = action_partial(s, m, ipart, level, threadIdx.x - a0, blockDim.x - a0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k == level - lo) v[4 + k] = a;
+    }
+  __syncthreads();
+  const int flags = m.ictl[C_FLAG];
+  double* out = m.vred + 8 * kWarps;
+  block_sum_vec(v, 8, m.vred, out);
+  if (threadIdx.x == 0)
+    for (int level = lo; level <= hi; ++level) {
+      llt[level] = out[hi - level];
+      lds[level] = out[4 + level - lo];
+      lnd[level] = ((flags >> level) & 1) ? 2e100 : 0.0;
+    }
+  __syncthreads();
+}
+
 
 // NT (largest block) and MINB set the register budget, 65536 / (NT * MINB)
 // per thread; the variants are compiled in separate translation units
@@ -777,17 +840,8 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         double* lds = m.red + kWarps + 8;  // [kMaxLevels] per level: action difference,
         double* llt = lds + kMaxLevels;     // mover ln T,
         double* lnd = llt + kMaxLevels;     // fixed-node difference
-        for (int level = L; level >= lb; --level) {
-          const uint32_t ubase = level_uniform_base(s, level);
-          const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
-          const double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
-          if (threadIdx.x == 0) {
-            lds[level] = ds;
-            llt[level] = lnT;
-            lnd[level] = 0.0;
-          }
-        }
-        if (mynode) node_level_range(s, m, scale[msp], msp, ipart, lb, L, cache, ifirst1, lnd);
+        top_levels(s, m, scale[msp], msp, ipart, lb, L, mynode, cache, ifirst1, P.seed, att, lds,
+                   llt, lnd);
         __syncthreads();
         if (threadIdx.x == 0) {
           double old = 0.0;

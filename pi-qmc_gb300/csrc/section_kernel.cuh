@@ -23,6 +23,7 @@ struct Smem {
   double *s2x, *s2y, *s2z;  // section 2 (fixed node)
   double *mx, *my, *mz;     // moving beads [nsec]
   double* red;              // reduction scratch
+  double* vred;             // vector reductions: [8][kWarps] partials, then 8 sums
   double* dm;               // [nspecies][nsec] determinants at section set-up
   double* ndm;              // [nsec] determinants of the moving species' new slices
   double* dist;             // [nsec][2][ns_max] distances at set-up (moving species)
