@@ -111,7 +111,7 @@ __device__ __forceinline__ double* group_cold(const Smem& m, int warp, int g, in
 // jcol < 0 fills it, jcol >= 0 reuses it and recomputes column jcol only (the
 // other columns' inputs are unchanged, so the values are bit-identical).
 template <int W>
-static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
+static __device__ __noinline__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
                                 int& err_out, double* d1, double* d2,
@@ -308,13 +308,20 @@ static __device__ void node_eval_group(const DevSys& s, int sp, const SliceView&
   for (int j = 0; j < n - 1; ++j) {  // forward: x(i) -= l(i,j) x(j), i > j
     // the columns nonzero at row j: order[q] for q <= j, rows j+1 .. n-1
     const int m = n - j - 1, cnt = (j + 1) * m;
+    int q = gl / m, ii = gl - q * m;  // element e = gl + k W: (q, row j + 1 + ii)
+    const int dq = W / m, di = W - dq * m;
     for (int e0 = 0; e0 < cnt; e0 += W) {
-      const int e = e0 + gl;
-      const int q = e < cnt ? e / m : 0;
-      const int c = __shfl_sync(FULL, ordc, q, W);
-      if (inv_ok && e < cnt) {
-        const int i = j + 1 + (e - q * m);
+      const bool on = e0 + gl < cnt;
+      const int c = __shfl_sync(FULL, ordc, on ? q : 0, W);
+      if (inv_ok && on) {
+        const int i = j + 1 + ii;
         X[c * n + i] -= A[j * n + i] * X[c * n + j];
+      }
+      ii += di;
+      q += dq;
+      if (ii >= m) {
+        ii -= m;
+        ++q;
       }
     }
     __syncwarp();
