@@ -148,7 +148,7 @@ static __device__ __noinline__ double ewald_level0_cached(const DevSys& s, const
   return sum * s.one_over_2v * s.tau / s.epsilon;
 }
 
-static __device__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
+static __device__ __noinline__ void load_section(const DevSys& s, const double* path, int ifirst, double* sx,
                              double* sy, double* sz) {
   const int np = s.npart, n = s.nsec * np;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
@@ -162,7 +162,7 @@ static __device__ void load_section(const DevSys& s, const double* path, int ifi
 }
 
 // SerialPaths::putBeads (src/base/SerialPaths.cc:143-185) with the identity permutation.
-static __device__ void store_section(const DevSys& s, double* path, int ifirst, const double* sx,
+static __device__ __noinline__ void store_section(const DevSys& s, double* path, int ifirst, const double* sx,
                               const double* sy, const double* sz) {
   const int np = s.npart, n = s.nsec * np;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
@@ -184,7 +184,7 @@ static __device__ void store_section(const DevSys& s, double* path, int ifirst, 
 // levels: moved slice `ord` (0 .. 2^L - 2 in FreeMover's order) takes Box-Muller
 // pairs 2 ord and 2 ord + 1 and uses the first three values (FP32 transform
 // in the mixed form).
-static __device__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t seed,
+static __device__ __noinline__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t seed,
                                        uint32_t rep, uint32_t att) {
   const int nord = (1 << s.nlevel) - 1;
   for (int o = threadIdx.x; o < nord; o += blockDim.x) {
@@ -206,7 +206,7 @@ static __device__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t 
   }
 }
 
-static __device__ double mover_level_part(const DevSys& s, const Smem& m, int ipart, int level,
+static __device__ __noinline__ double mover_level_part(const DevSys& s, const Smem& m, int ipart, int level,
                               uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
@@ -365,7 +365,7 @@ __device__ __forceinline__ double* cache_entry(const DevSys& s, double* cache, i
 // or of all of them (only_sp < 0): cached results are copied, the others are
 // evaluated, the species' warps side by side.  Determinants go to dm[sp][t],
 // error flags to errs[sp][t], the moving species' distances to dist.
-static __device__ void node_init_pass(const DevSys& s, const Smem& m, const double* scale,
+static __device__ __noinline__ void node_init_pass(const DevSys& s, const Smem& m, const double* scale,
                                       const int* epoch, int msp, double* cache, int ifirst1,
                                       int only_sp, int start) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
@@ -459,7 +459,7 @@ static __device__ void node_init_pass(const DevSys& s, const Smem& m, const doub
 // other; they are independent); at a species' first slice whose determinant
 // leaves [1e-50, 1e50] its loop is replayed sequentially, and its later
 // slices are re-evaluated.
-static __device__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
+static __device__ __noinline__ void node_initialize(const DevSys& s, const Smem& m, double* scale, int* epoch,
                                 int msp, uint32_t* status, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nsec = s.nsec, M = s.nslice;
@@ -548,7 +548,7 @@ static __device__ void node_initialize(const DevSys& s, const Smem& m, double* s
 
 // FixedNodeAction::getActionDifference (src/fixednode/FixedNodeAction.cc:39-131)
 // for the moving species at one level.
-static __device__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
+static __device__ __noinline__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
                              int level, double* cache, int ifirst1) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max;
@@ -645,14 +645,14 @@ __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int leve
 // the action difference, llt[l] the mover's ln(T_old/T_new), lnd[l] the
 // fixed-node difference (2e100 when a changed slice crosses a node, else 0).
 // The caller applies pi-qmc's level-by-level decisions to them.
-static __device__ void top_levels(const DevSys& s, const Smem& m, double scale, int msp,
+static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, double scale, int msp,
                                   int ipart, int lo, int hi, bool mynode, double* cache,
                                   int ifirst1, uint64_t seed, uint32_t att, double* lds,
                                   double* llt, double* lnd) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
-  const int nb = hi - lo + 1;  // <= 4
-  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // [0, nb): mover terms, [4, 4 + nb): action terms
+  // hi - lo + 1 <= 4 levels: v[0..3] mover terms, v[4..7] action terms
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int level = hi; level >= lo; --level) {
     const double p = mover_level_part(s, m, ipart, level, seed, s.stream_id, att,
                                       level_uniform_base(s, level));

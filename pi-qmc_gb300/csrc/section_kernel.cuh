@@ -463,7 +463,7 @@ static __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& 
 // (src/action/PrimSHOAction.cc:21-58), PairAction per species pair
 // (src/action/PairAction.cc:219-360).  Work items are links and (partner, link)
 // pairs; each item contributes (new - old).
-static __device__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level,
+static __device__ __noinline__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level,
                                         int tid, int nthreads) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
