@@ -274,8 +274,11 @@ int pimc_ewald_coefficients(double* coef, int n);
 /* ---- launch configuration and autotuning -------------------------------- */
 
 /* Launch configuration of an engine's section kernel: threads per replica
- * (64, 128, 256, or 512 with variant 1), the per-warp Slater scratch in shared (0) or global (1)
- * memory, the replicas resident per SM (0: as many as fit) and the section
+ * (64, 128, 256, or 512 with variant 1), where the per-warp Slater scratch lives (0: shared
+ * memory where it fits; 1: global memory; 2: its hot part, the LU and inverse, in shared
+ * memory and its cold part, the element and gradient matrices, in global memory, which
+ * frees shared memory for more resident replicas), the replicas resident per SM (0: as
+ * many as fit) and the section
  * kernel's register-budget variant.  ms is the
  * time the autotuner measured for it (0 when not measured).  A configuration
  * changes how per-thread partial sums are grouped, so chains run under two

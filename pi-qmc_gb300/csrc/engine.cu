@@ -104,6 +104,7 @@ struct DevBuf {
 // Layout choices the autotuner varies.
 struct LayoutOpts {
   bool scratch_global = false;  // per-warp Slater scratch in global memory even when it fits
+  bool cold_global = false;     // its cold parts in global memory even when all of it fits
   bool full_ewald_tables = false;  // Ewald tables for every bead (full evalLongRange sums)
 };
 
@@ -426,7 +427,8 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   } else {
     const int cand[5][3] = {  // {ncol in smem, per-warp scratch in smem, split}
         {1, full, 0}, {1, hot, 1}, {0, hot, 1}, {1, 0, 0}, {0, 0, 0}};
-    for (int c = opts.scratch_global ? kGlobalCol : kAll; c <= kGlobal; ++c)
+    const int first = opts.scratch_global ? kGlobalCol : (opts.cold_global ? kHotCol : kAll);
+    for (int c = first; c <= kGlobal; ++c)
       if (base + (cand[c][0] ? ncol_size : 0) + nwarps * cand[c][1] <= limit || c == kGlobal) {
         place = c;
         break;
@@ -1514,15 +1516,18 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
 
 int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg) {
   if (!e || e->server || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
+  if (cfg->scratch_global < 0 || cfg->scratch_global > 2)
+    return fail(PIMC_ERR_INVALID, "scratch_global must be 0, 1 or 2");
   LayoutOpts o;
-  o.scratch_global = cfg->scratch_global != 0;
+  o.scratch_global = cfg->scratch_global == 1;
+  o.cold_global = cfg->scratch_global == 2;
   return apply_config(e, cfg->block, o, cfg->ctas_per_sm, cfg->regs_variant ? cfg->regs_variant : 2);
 }
 
 int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg) {
   if (!e || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
   cfg->block = e->block;
-  cfg->scratch_global = e->lay_opts.scratch_global ? 1 : 0;
+  cfg->scratch_global = e->lay_opts.scratch_global ? 1 : (e->lay_opts.cold_global ? 2 : 0);
   cfg->ctas_per_sm = e->ctas_cap;
   cfg->regs_variant = e->minb;
   cfg->ms = 0.f;
@@ -1562,15 +1567,16 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   std::vector<pimc_launch_config> cand;
   for (int v : {2, 3, 4})
     for (int b : {64, 128, 256})
-      for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
-  for (int g = 0; g < (fixed ? 2 : 1); ++g) cand.push_back({512, g, 0, 1, 0.f});
+      for (int g = 0; g < (fixed ? 3 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
+  for (int g = 0; g < (fixed ? 3 : 1); ++g) cand.push_back({512, g, 0, 1, 0.f});
   cudaEvent_t t0, t1;
   CU(cudaEventCreate(&t0));
   CU(cudaEventCreate(&t1));
   int nt = 0, ibest = -1;
   for (pimc_launch_config& c : cand) {
     LayoutOpts o;
-    o.scratch_global = c.scratch_global != 0;
+    o.scratch_global = c.scratch_global == 1;
+    o.cold_global = c.scratch_global == 2;
     if (apply_config(e, c.block, o, c.ctas_per_sm, c.regs_variant) != PIMC_OK) {
       c.ms = -1.f;  // does not fit
       continue;

@@ -273,6 +273,7 @@ def test_graph_steps_equal_direct_calls(pimc):
 
 @pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small"])
 @pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 4), (128, 1, 3), (256, 1, 2),
+                                                       (256, 2, 3), (128, 2, 2),
                                                        (256, 0, 3), (512, 1, 1), (512, 0, 1)])
 def test_launch_configs_match_golden(pimc, case, block, scratch_global, regs):
     # Every launch configuration the autotuner may pick reproduces pi-qmc's
@@ -293,7 +294,7 @@ def test_launch_configs_match_golden(pimc, case, block, scratch_global, regs):
 
 
 @pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 2), (128, 0, 2), (256, 0, 2),
-                                                       (512, 0, 1), (256, 1, 2)])
+                                                       (512, 0, 1), (256, 1, 2), (256, 2, 2)])
 def test_electron_gas_scratch_placements(pimc, block, scratch_global, regs):
     # 27 x 27 free-particle matrices: every shared-memory placement of the Slater
     # scratch (whole, hot part with the cold part and the new-column buffer in
