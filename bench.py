@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--sweep-scale", type=float, default=1e-5,
                    help="serve: factor on the requested sweeps (log-uniform 1e3..1e5)")
     p.add_argument("--slots", type=int, default=1024, help="serve: concurrent simulations")
+    p.add_argument("--server-block", type=int, default=256, help="serve: threads per simulation")
+    p.add_argument("--server-scratch", type=int, default=0,
+                   help="serve: Slater scratch placement (0 shared, 1 global, 2 split)")
     p.add_argument("--pool-gb", type=float, default=32.0, help="serve: device pool for paths")
     p.add_argument("--round-budget", type=float, default=1.0,
                    help="serve: round length in units of 8 attempts of the largest system")
@@ -299,6 +302,7 @@ def run_serve(args, rank, world):
     seed = rank_seed(rank)
     pool = int(args.pool_gb * (1 << 30))
     srv = pimc_gb300.Server(args.slots, pool, 64, 2048, 5, 32, seed=seed, precision=prec)
+    srv.configure(args.server_block, args.server_scratch, 2)
     stream = torch.cuda.current_stream()
     srv.set_stream(stream.cuda_stream)
     # warm-up: a short stream served all at once (untimed)
@@ -335,6 +339,7 @@ def run_serve(args, rank, world):
                            "then its energy is measured",
                    "requests": args.requests, "rate_per_s": args.rate,
                    "sweep_scale": args.sweep_scale, "slots": args.slots,
+                   "server_block": args.server_block, "server_scratch": args.server_scratch,
                    "pool_bytes": pool, "precision": args.precision,
                    "offered_bead_updates_per_s": offered,
                    "l2": "request paths and Slater caches (GBs in total) exceed L2",

@@ -292,6 +292,9 @@ typedef struct {
   float ms;
 } pimc_launch_config;
 
+/* On a server the configuration (block, scratch placement, register variant)
+ * applies to every round and may be set only before the first admission, so
+ * that a simulation's sums never depend on the mix it is served in. */
 int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg);
 int pimc_engine_get_config(pimc_engine* e, pimc_launch_config* cfg);
 /* Times each candidate configuration on nattempt section attempts per replica

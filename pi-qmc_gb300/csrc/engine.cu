@@ -1515,9 +1515,26 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
 }  // namespace
 
 int pimc_engine_configure(pimc_engine* e, const pimc_launch_config* cfg) {
-  if (!e || e->server || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
+  if (!e || !cfg) return fail(PIMC_ERR_INVALID, "bad argument");
   if (cfg->scratch_global < 0 || cfg->scratch_global > 2)
     return fail(PIMC_ERR_INVALID, "scratch_global must be 0, 1 or 2");
+  if (e->server) {
+    // a server's block size is fixed while it serves (a slot's sums must not
+    // depend on the mix): set it before the first admission
+    if (e->nactive > 0) return fail(PIMC_ERR_INVALID, "configure a server before admitting");
+    for (int r = 0; r < e->nrep; ++r)
+      if (e->active[r]) return fail(PIMC_ERR_INVALID, "configure a server before admitting");
+    const int minb = cfg->regs_variant ? cfg->regs_variant : 2;
+    if (!((cfg->block == 64 || cfg->block == 128 || cfg->block == 256) && minb >= 2 && minb <= 4) &&
+        !(cfg->block == 512 && minb == 1))
+      return fail(PIMC_ERR_INVALID, "block must be 64, 128, 256 (or 512 with variant 1)");
+    e->block = cfg->block;
+    e->minb = minb;
+    e->lay_opts.scratch_global = cfg->scratch_global == 1;
+    e->lay_opts.cold_global = cfg->scratch_global == 2;
+    e->order_dirty = true;
+    return PIMC_OK;
+  }
   LayoutOpts o;
   o.scratch_global = cfg->scratch_global == 1;
   o.cold_global = cfg->scratch_global == 2;
@@ -1670,7 +1687,7 @@ int refresh_order(pimc_engine* e) {
     // shared-memory layout and grid sized to the systems now admitted; the
     // block size stays fixed so that a slot's arithmetic never depends on the mix
     bool ok = false;
-    e->lay = make_layout(live, e->block / 32, ok);
+    e->lay = make_layout(live, e->block / 32, ok, e->lay_opts);
     if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
     int occ = 1;
     occ = section_occupancy(e->minb, e->block, e->lay.total * 8);

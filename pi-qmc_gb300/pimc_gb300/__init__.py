@@ -545,6 +545,11 @@ class Server(_Checkpoint):
         except Exception:
             pass
 
+    def configure(self, block=256, scratch_global=0, regs_variant=2):
+        """Launch shape of every round (before the first admission)."""
+        cfg = LaunchConfig(block, scratch_global, 0, regs_variant, 0.0)
+        _check(lib().pimc_engine_configure(self.h, C.byref(cfg)))
+
     def set_stream(self, stream_ptr):
         _check(lib().pimc_set_stream(self.h, C.c_void_p(stream_ptr)))
 
