@@ -819,21 +819,33 @@ int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) 
   P.nslot = nslot;
   P.ntask_per_slot = nsp * mmax;
   P.stage_stride = (6 * nmax + 1) & ~1;
-  P.scratch_stride = (node_group_scratch(nmax, anyfree) + 1) & ~1;
-  // Slater scratch in shared memory up to 6 KB a warp, else in global memory
-  const bool gscr = P.scratch_stride * 8 > 6 * 1024;
+  // Slater scratch: all of it in shared memory up to 6 KB a warp; else its hot
+  // part (LU, inverse) there up to 24 KB with the cold part in global memory;
+  // else all of it in global memory
+  const int full = (node_group_scratch(nmax, anyfree) + 1) & ~1;
+  const int hot = (node_group_hot(nmax) + 1) & ~1;
+  const int cold = (node_group_cold(nmax, anyfree) + 1) & ~1;
+  const bool all_smem = full * 8 <= 6 * 1024, split = !all_smem && hot * 8 <= 24 * 1024;
+  P.scratch_stride = split ? hot : full;
+  P.cold_stride = split ? cold : 0;
   const int nw = kBlock / 32;
-  const size_t smem = (size_t)nw * (P.stage_stride + (gscr ? 0 : P.scratch_stride)) * 8;
+  const size_t smem =
+      (size_t)nw * (P.stage_stride + ((all_smem || split) ? P.scratch_stride : 0)) * 8;
   const long long ntask = (long long)nslot * P.ntask_per_slot;
   const int grid = (int)std::min<long long>((ntask + nw - 1) / nw, (long long)e->num_sms * 4);
   P.gscratch = nullptr;
-  if (gscr) {
-    const size_t need = (size_t)grid * nw * P.scratch_stride;
+  P.gcold = nullptr;
+  const size_t gper = all_smem ? 0 : (split ? (size_t)cold : (size_t)full);
+  if (gper) {
+    const size_t need = (size_t)grid * nw * gper;
     if (e->d_prefill_scr.n < need) {
       CU(cudaStreamSynchronize(e->stream));  // an earlier fill may still use it
       if (e->d_prefill_scr.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc prefill scratch");
     }
-    P.gscratch = e->d_prefill_scr.p;
+    if (split)
+      P.gcold = e->d_prefill_scr.p;
+    else
+      P.gscratch = e->d_prefill_scr.p;
   }
   cudaFuncSetAttribute(cache_prefill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        200 * 1024);

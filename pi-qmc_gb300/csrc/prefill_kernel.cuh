@@ -19,14 +19,17 @@ struct PrefillParams {
   int nslot;
   int ntask_per_slot;  // nspecies_max x nslice_max
   int stage_stride;    // doubles of slice-pair staging per warp (6 n_max)
-  int scratch_stride;  // doubles of Slater scratch per warp
+  int scratch_stride;  // doubles of Slater scratch per warp (its hot part when split)
   double* gscratch;    // per-warp Slater scratch in global memory (null: shared memory)
+  double* gcold;       // per-warp cold parts in global memory when split (null: not split)
+  int cold_stride;     // doubles of cold part per warp
 };
 
 // Warps loop over the (slot, species, slice) entries; shared memory holds each
-// warp's staged slice pair, and its Slater scratch too unless that is large
-// (27 x 27 free-particle matrices: 35 KB a warp), when the scratch lives in
-// global memory so that more warps stay resident.
+// warp's staged slice pair and its Slater scratch, or, for large matrices
+// (27 x 27 free-particle matrices: 35 KB a warp), the scratch's hot part (LU
+// and inverse) with the cold part (element and gradient matrices) in global
+// memory, so that more warps stay resident.
 __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) {
   extern __shared__ double sh[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
@@ -35,6 +38,7 @@ __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) 
   double* st = sh + (size_t)warp * P.stage_stride;
   double* scr = P.gscratch ? P.gscratch + gw * P.scratch_stride
                            : sh + (size_t)nwarps * P.stage_stride + (size_t)warp * P.scratch_stride;
+  double* cold = P.gcold ? P.gcold + gw * P.cold_stride : nullptr;
   const long long ntask = (long long)P.nslot * P.ntask_per_slot;
   for (long long task = gw; task < ntask; task += nwt) {  // warp-uniform
     const int k = (int)(task / P.ntask_per_slot), tk = (int)(task % P.ntask_per_slot);
@@ -68,7 +72,7 @@ __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) 
     double det = 0;
     int err = 0;
     node_eval_group<32>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err, e + 2,
-                        e + 2 + n, nullptr, 0xffffffffu);
+                        e + 2 + n, nullptr, 0xffffffffu, cold);
     __syncwarp();
     if (lane == 0) {
       e[1] = det;
