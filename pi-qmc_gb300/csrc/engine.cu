@@ -379,7 +379,6 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.q = take(np);
   L.dm = take(kMaxSpecies * nsec);
   L.ndm = take(nsec);
-  L.edet = take(nsec);
   L.dist = take(fixed ? nsec * 2 * nsm : 0);
   L.ndist = take(fixed ? nsec * 2 * nsm : 0);
   L.ewt = take(2 * per * L.ewt_cols);
@@ -488,7 +487,7 @@ Layout estimator_layout(const std::vector<DevSys>& sys, const int* ikmax_extra) 
   L.q = take(np);
   L.ewt = take(2 * ((ik[0] + 1) + (2 * ik[1] + 1) + (2 * ik[2] + 1)) * (np + 1));
   L.ictl = take(C_NCTL + 2);
-  L.dm = L.ndm = L.edet = L.dist = L.ndist = L.red;
+  L.dm = L.ndm = L.dist = L.ndist = L.red;
   L.ecache = L.ncol = -1;
   L.nodescr = 0;
   L.nodescr_in_smem = 1;

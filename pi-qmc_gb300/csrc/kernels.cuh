@@ -9,7 +9,7 @@ namespace pimc {
 // Offsets (in doubles) of the shared-memory working set; computed on the host
 // for the largest replica of a launch.
 struct Layout {
-  int s1, s2, mv, red, q, dm, ndm, edet, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
+  int s1, s2, mv, red, q, dm, ndm, dist, ndist, ewt, nodescr, ictl, ecache, ncol;
   int ncol_stride;
   int nrm;  // the attempt's normals, 3 per movable slice
   int vred;             // vector reductions: [8][kWarps] partials, then 8 sums
@@ -60,7 +60,6 @@ __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSy
   m.qpart = base + L.q;
   m.dm = base + L.dm;
   m.ndm = base + L.ndm;
-  m.edet = base + L.edet;
   m.dist = base + L.dist;
   m.ndist = base + L.ndist;
   m.ewt = base + L.ewt;
@@ -397,8 +396,7 @@ static __device__ __noinline__ void node_init_pass(const DevSys& s, const Smem& 
   __syncthreads();
   // warp tasks: each warp takes up to G misses of one species (lane groups of
   // a warp must run the same species so that they stay converged)
-  int total = 0, ntask = 0;
-  for (int sp = 0; sp < s.nspecies; ++sp) total += nmiss[sp];
+  int ntask = 0;
   int Gs[kMaxSpecies], Ws[kMaxSpecies], first[kMaxSpecies + 1];
   for (int sp = 0; sp < s.nspecies; ++sp) {
     Ws[sp] = node_group_width(s.spec_count[sp]);

@@ -99,29 +99,36 @@ __device__ __forceinline__ void pbc(const DevSys& s, double& x, double& y, doubl
   }
 }
 
-// PeriodicGaussian::evaluate (src/util/PeriodicGaussian.cc:20-40): theta series
-// value and gradient.
+// PeriodicGaussian::evaluate (src/util/PeriodicGaussian.cc:20-40): the theta
+// series value pref (1 + 2 sum_n q^(n^2) cos(n k x)) and its gradient
+// -2 pref k sum_n n q^(n^2) sin(n k x), n < nmax.  pi-qmc builds the terms by a
+// complex recurrence (q^(2n-1) e^(ikx) per step); here cos(n k x) and
+// sin(n k x) follow the Chebyshev recurrence t_(n+1) = 2 cos(kx) t_n - t_(n-1)
+// and the weights q^(n^2) the product q^(n^2) q^(2n+1): seven FP64 operations
+// a term instead of fourteen, the same sums to ~1e-13 relative where the
+// series nearly cancels (far smaller elsewhere).  Rounded operations
+// throughout: every call site computes the same bits.
 __device__ __forceinline__ double pg_eval(double nome, double pref, double k, int nmax, double x,
                                           double* grad) {
   double sw, cw;
   sincos(__dmul_rn(k, x), &sw, &cw);
-  // (rounded operations throughout: every call site computes the same bits)
-  double tr = 1.0, ti = 0.0;  // term
-  double s0r = 0.0, s1r = 0.0;
-  double nomeN = 1.0;
+  const double c2 = __dmul_rn(2.0, cw), q2 = __dmul_rn(nome, nome);
+  double cp = 1.0, cc = cw, sp = 0.0, sc = sw;  // cos, sin of (n - 1) k x and n k x
+  double w = nome, step = nome;                  // q^(n^2), q^(2n - 1)
+  double s0 = 0.0, s1 = 0.0;
   for (int n = 1; n < nmax; ++n) {
-    const double f = __dmul_rn(__dmul_rn(nomeN, nomeN), nome);
-    const double fr = __dmul_rn(f, cw), fi = __dmul_rn(f, sw);
-    const double nr = __dsub_rn(__dmul_rn(tr, fr), __dmul_rn(ti, fi));
-    const double ni = __dadd_rn(__dmul_rn(tr, fi), __dmul_rn(ti, fr));
-    tr = nr;
-    ti = ni;
-    s0r = __dadd_rn(s0r, tr);
-    s1r = __dadd_rn(s1r, __dmul_rn(__dmul_rn(-ti, k), double(n)));  // real(term * i k * n)
-    nomeN = __dmul_rn(nomeN, nome);
+    s0 = __fma_rn(w, cc, s0);
+    s1 = __fma_rn(__dmul_rn(double(n), w), sc, s1);
+    step = __dmul_rn(step, q2);
+    w = __dmul_rn(w, step);
+    const double cn = __fma_rn(c2, cc, -cp), sn = __fma_rn(c2, sc, -sp);
+    cp = cc;
+    cc = cn;
+    sp = sc;
+    sc = sn;
   }
-  *grad = __dmul_rn(__dmul_rn(pref, 2.0), s1r);
-  return __dmul_rn(pref, __dadd_rn(1.0, __dmul_rn(2.0, s0r)));
+  *grad = __dmul_rn(__dmul_rn(__dmul_rn(pref, 2.0), -k), s1);
+  return __dmul_rn(pref, __fma_rn(2.0, s0, 1.0));
 }
 
 // Pair-action table lookup on the logarithmic grid

@@ -28,7 +28,6 @@ struct Smem {
   double* ndm;              // [nsec] determinants of the moving species' new slices
   double* dist;             // [nsec][2][ns_max] distances at set-up (moving species)
   double* ndist;            // [nsec][2][ns_max] distances of the new path
-  double* edet;             // [nsec] speculative determinants during set-up
   double* ewt;              // Ewald exp(ik.r) tables: [kx, ky, kz rows][ewt_cols]
   double* qpart;            // [npart] charges
   int* ictl;                // control words
