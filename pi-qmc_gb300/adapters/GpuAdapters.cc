@@ -1,11 +1,15 @@
 #include "GpuAdapters.h"
 
+#include <cstring>
 #include <stdexcept>
 #include <string>
 
 #include "advancer/SectionSamplerInterface.h"
 #include "base/Beads.h"
 #include "base/Paths.h"
+#include "base/SimulationInfo.h"
+#include "base/Species.h"
+#include "util/SuperCell.h"
 
 namespace pimc_gb300 {
 
@@ -97,6 +101,35 @@ double gpuThermoEnergy(const Paths& paths, pimc_engine* engine) {
   double e = 0;
   check(pimc_thermo_energy(engine, &e), "pimc_thermo_energy");
   return e;
+}
+
+pimc_system systemFromSimulation(const SimulationInfo& simInfo, const SystemOptions& opt) {
+  pimc_system sys;
+  memset(&sys, 0, sizeof(sys));
+  sys.npart = simInfo.getNPart();
+  sys.nspecies = simInfo.getNSpecies();
+  if (sys.nspecies > PIMC_MAX_SPECIES) throw std::runtime_error("too many species");
+  for (int i = 0; i < sys.nspecies; ++i) {
+    const Species& sp = simInfo.getSpecies(i);
+    sys.spec_count[i] = sp.count;
+    sys.spec_mass[i] = sp.mass;
+    sys.spec_charge[i] = sp.charge;
+    sys.sho_omega[i] = i < (int)opt.sho_omega.size() ? opt.sho_omega[i] : 0.0;
+    sys.node_kind[i] = i < (int)opt.node_kind.size() ? opt.node_kind[i] : PIMC_NODES_NONE;
+    sys.node_omega[i] = i < (int)opt.node_omega.size() ? opt.node_omega[i] : 0.0;
+  }
+  sys.node_temperature = opt.node_temperature > 0 ? opt.node_temperature : simInfo.getTemperature();
+  sys.nslice = simInfo.getNSlice();
+  sys.tau = simInfo.getTau();
+  sys.nlevel = opt.nlevel;
+  const SuperCell& cell = *simInfo.getSuperCell();
+  for (int d = 0; d < NDIM; ++d) sys.cell[d] = cell[d];
+  sys.spring = opt.spring ? 1 : 0;
+  sys.coulomb = opt.coulomb ? 1 : 0;
+  sys.epsilon = opt.epsilon;
+  sys.ewald = opt.ewald ? 1 : 0;
+  sys.mover = opt.pbc_mover ? PIMC_MOVER_FREE_PBC : PIMC_MOVER_FREE;
+  return sys;
 }
 
 }  // namespace pimc_gb300

@@ -26,6 +26,7 @@
 
 class Paths;
 class SectionSamplerInterface;
+class SimulationInfo;
 
 namespace pimc_gb300 {
 
@@ -87,6 +88,26 @@ class GpuSectionSampler : public Algorithm {
 // ThermoEnergyEstimator's value (src/estimator/ThermoEnergyEstimator.cc:32-66)
 // for pi-qmc's current paths, computed on the device.
 double gpuThermoEnergy(const Paths& paths, pimc_engine* engine);
+
+// The attributes pi-qmc's parsers read for the actions, node models and
+// sampler of this path (src/parser/ActionParser.cc:105-153,433-452,
+// src/parser/PIMCParser.cc:312-491) that SimulationInfo does not hold.
+struct SystemOptions {
+  int nlevel = 5;                  // <Sample nlevel=...>
+  bool spring = true;              // <SpringAction/>
+  bool coulomb = false;            // <CoulombAction/> (pair tables needed)
+  bool ewald = false;              // <CoulombAction ewald="true"/> (Ewald table needed)
+  bool pbc_mover = false;          // FreeMoverPBC instead of FreeMover
+  double epsilon = 1.0;            // dielectric constant
+  std::vector<double> sho_omega;   // <SHOAction omega=...> per species (empty or 0: none)
+  std::vector<int> node_kind;      // PIMC_NODES_* per species (<FixedNodeAction model=...>)
+  std::vector<double> node_omega;  // SHONodes omega per species
+  double node_temperature = 0;     // trial density matrix temperature (0: the simulation's)
+};
+
+// The engine's description of pi-qmc's system: species, masses and charges,
+// slices, tau and cell from SimulationInfo, the rest from the options.
+pimc_system systemFromSimulation(const SimulationInfo& simInfo, const SystemOptions& opt);
 
 }  // namespace pimc_gb300
 #endif
