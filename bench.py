@@ -336,7 +336,8 @@ def run_serve(args, rank, world):
         "config": {"workload": "serve: " + describe("serve"),
                    "step": "one serving round: every admitted simulation advances its own "
                            "attempts (about equal device time each; 8 for N=64 at level 5), "
-                           "then its energy is measured",
+                           "then the simulations that completed a sweep or their request "
+                           "are measured",
                    "requests": args.requests, "rate_per_s": args.rate,
                    "sweep_scale": args.sweep_scale, "slots": args.slots,
                    "server_block": args.server_block, "server_scratch": args.server_scratch,

@@ -339,6 +339,10 @@ int pimc_server_release(pimc_engine* e, int slot);
 int pimc_server_run(pimc_engine* e);
 /* Thermodynamic energy of every admitted slot (NaN for free slots). */
 int pimc_server_energy(pimc_engine* e, double* energy /* slots */);
+/* The same for the listed active slots only (energy[k] for slots[k]): a
+ * serving loop measures a simulation once per sweep and at its end, not
+ * every round.  A slot's value does not depend on which slots are listed. */
+int pimc_server_energy_slots(pimc_engine* e, const int* slots, int nslot, double* energy);
 int pimc_server_download_path(pimc_engine* e, int slot, double* host_xyz);
 /* Bytes of the pool in use and free (largest free block). */
 int pimc_server_pool(pimc_engine* e, size_t* used, size_t* largest_free);

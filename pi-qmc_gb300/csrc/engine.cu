@@ -1934,40 +1934,70 @@ int pimc_server_run(pimc_engine* e) {
   return PIMC_OK;
 }
 
-int pimc_server_energy(pimc_engine* e, double* energy) {
-  if (!e || !e->server || !energy) return fail(PIMC_ERR_INVALID, "bad argument");
-  if (int rc = refresh_order(e)) return rc;
-  for (int r = 0; r < e->nrep; ++r) energy[r] = std::nan("");
-  if (e->nactive == 0) return PIMC_OK;
+}  // extern "C"
+
+namespace {
+// ThermoEnergyEstimator's value for the listed slots (host list) into out[k].
+int server_energy(pimc_engine* e, const std::vector<int>& slots, double* out) {
+  const int n = (int)slots.size();
+  if (n == 0) return PIMC_OK;
   // a fixed chunk count: each slot's sum is grouped the same way whatever the mix
   const int nchunk = 64;
   double* d_part = nullptr;
-  CU(cudaMallocAsync(&d_part, sizeof(double) * (size_t)e->nactive * nchunk, e->stream));
+  int* d_idx = nullptr;
+  CU(cudaMallocAsync(&d_part, sizeof(double) * (size_t)n * nchunk, e->stream));
+  CU(cudaMallocAsync(&d_idx, sizeof(int) * (size_t)n, e->stream));
+  CU(cudaMemcpyAsync(d_idx, slots.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                     e->stream));
   ThermoParams P;
   P.sys = e->d_sys.p;
-  P.index = e->d_order.p;
+  P.index = d_idx;
   P.paths = e->d_pool.p;
   P.ekcache = nullptr;  // servers take no Ewald systems
   P.partial = d_part;
   P.nchunk = nchunk;
-  P.nrep = e->nactive;
+  P.nrep = n;
   P.lay = e->lay;
-  thermo_kernel<<<dim3(nchunk, e->nactive), kBlock, e->lay.total * 8, e->stream>>>(P);
+  thermo_kernel<<<dim3(nchunk, n), kBlock, e->lay.total * 8, e->stream>>>(P);
   e->launches++;
   CU(cudaGetLastError());
-  std::vector<double> part((size_t)e->nactive * nchunk);
-  std::vector<int> order(e->nactive);
+  std::vector<double> part((size_t)n * nchunk);
   CU(cudaMemcpyAsync(part.data(), d_part, part.size() * 8, cudaMemcpyDeviceToHost, e->stream));
-  CU(cudaMemcpyAsync(order.data(), e->d_order.p, order.size() * 4, cudaMemcpyDeviceToHost,
-                     e->stream));
   CU(cudaFreeAsync(d_part, e->stream));
+  CU(cudaFreeAsync(d_idx, e->stream));
   CU(cudaStreamSynchronize(e->stream));
-  for (int k = 0; k < e->nactive; ++k) {
+  for (int k = 0; k < n; ++k) {
     double s = 0;
     for (int c = 0; c < nchunk; ++c) s += part[(size_t)k * nchunk + c];
-    energy[order[k]] = s / e->hsys[order[k]].nslice;
+    out[k] = s / e->hsys[slots[k]].nslice;
   }
   return PIMC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pimc_server_energy(pimc_engine* e, double* energy) {
+  if (!e || !e->server || !energy) return fail(PIMC_ERR_INVALID, "bad argument");
+  if (int rc = refresh_order(e)) return rc;
+  for (int r = 0; r < e->nrep; ++r) energy[r] = std::nan("");
+  std::vector<int> slots;
+  for (int r = 0; r < e->nrep; ++r)
+    if (e->active[r]) slots.push_back(r);
+  std::vector<double> out(slots.size());
+  if (int rc = server_energy(e, slots, out.data())) return rc;
+  for (size_t k = 0; k < slots.size(); ++k) energy[slots[k]] = out[k];
+  return PIMC_OK;
+}
+
+int pimc_server_energy_slots(pimc_engine* e, const int* slots, int nslot, double* energy) {
+  if (!e || !e->server || nslot < 0 || (nslot > 0 && (!slots || !energy)))
+    return fail(PIMC_ERR_INVALID, "bad argument");
+  for (int k = 0; k < nslot; ++k)
+    if (slots[k] < 0 || slots[k] >= e->nrep || !e->active[slots[k]])
+      return fail(PIMC_ERR_INVALID, "slot not in use");
+  if (int rc = refresh_order(e)) return rc;
+  return server_energy(e, std::vector<int>(slots, slots + nslot), energy);
 }
 
 int pimc_server_download_path(pimc_engine* e, int slot, double* host_xyz) {

@@ -180,6 +180,7 @@ def lib():
         L.pimc_server_release.argtypes = [P, I]
         L.pimc_server_run.argtypes = [P]
         L.pimc_server_energy.argtypes = [P, D]
+        L.pimc_server_energy_slots.argtypes = [P, C.POINTER(C.c_int), I, D]
         L.pimc_server_download_path.argtypes = [P, I, D]
         L.pimc_server_pool.argtypes = [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.pimc_kernel_launches.argtypes = [P]
@@ -577,9 +578,18 @@ class Server(_Checkpoint):
         """One round: every slot advances its own round_attempts."""
         _check(lib().pimc_server_run(self.h))
 
-    def energies(self):
-        out = np.empty(self.slots)
-        _check(lib().pimc_server_energy(self.h, _dp(out)))
+    def energies(self, slots=None):
+        """Thermodynamic energy of every slot (NaN for free slots), or of the
+        listed active slots only (in that order)."""
+        if slots is None:
+            out = np.empty(self.slots)
+            _check(lib().pimc_server_energy(self.h, _dp(out)))
+            return out
+        idx = np.ascontiguousarray(slots, np.int32)
+        out = np.empty(len(idx))
+        if len(idx):
+            _check(lib().pimc_server_energy_slots(self.h, idx.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  len(idx), _dp(out)))
         return out
 
     def download_path(self, slot):

@@ -6,7 +6,9 @@ slot of a :class:`pimc_gb300.Server` as soon as a slot and device memory for its
 path and Slater-result cache are free (first fit over the waiting requests in
 arrival order), then runs one round: every admitted simulation advances its own
 number of section attempts in one persistent launch, then the thermodynamic
-energy of every slot is measured.  Simulations that have done their attempts
+energy is measured for the slots that completed a sweep (ceil(M / 2^L) N
+attempts, pi-qmc's measurement interval) or their whole request in that
+round.  Simulations that have done their attempts
 leave and free their slots for the next arrivals.  Work of requests that
 arrive while others run overlaps on the device.
 
@@ -111,6 +113,22 @@ class ServeLoop:
         ra = self.round_attempts(req)
         return max(1, -(-req.attempts // ra))
 
+    @staticmethod
+    def sweep(req):
+        """Section attempts of one sweep: ceil(M / 2^L) sections x N particles."""
+        kw = req.system_kw
+        return -(-kw["nslice"] // (1 << kw["nlevel"])) * sum(kw["counts"])
+
+    def samples_for(self, req):
+        """Energy samples a request gets: one per completed sweep, and one at its end."""
+        ra, sw = self.round_attempts(req), self.sweep(req)
+        n, done = 0, 0
+        for _ in range(self.rounds_for(req)):
+            prev, done = done, done + ra
+            if done >= req.attempts or done // sw > prev // sw:
+                n += 1
+        return n
+
     def run(self, requests, realtime=True):
         """Serves `requests` (sorted by arrival).  With `realtime`, a request
         is admitted no earlier than its arrival time after the start; without,
@@ -148,13 +166,20 @@ class ServeLoop:
                 continue
             tb = self.clock()
             self.server.run()
-            e = self.server.energies()
+            due = []
+            for slot, r in active.items():
+                prev = r.done
+                r.done += r.round_attempts
+                sw = self.sweep(r)
+                if r.done >= r.attempts or r.done // sw > prev // sw:
+                    due.append(slot)
+            e = self.server.energies(due)
             self.busy += self.clock() - tb
             self.rounds += 1
+            for k, slot in enumerate(due):
+                active[slot].energies.append(float(e[k]))
             for slot in list(active):
                 r = active[slot]
-                r.done += r.round_attempts
-                r.energies.append(float(e[slot]))
                 if r.done >= r.attempts:
                     if self.keep_paths:
                         r.final_path = self.server.download_path(slot)

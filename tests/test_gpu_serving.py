@@ -54,6 +54,7 @@ def test_server_slot_follows_engine_replica(base_tables):
         e1 = eng.thermo_energy()[0]
         e2 = srv.energies()[slot]
         assert abs(e1 - e2) <= 1e-12 * abs(e1)
+        assert srv.energies([slot])[0] == e2  # measuring a subset gives the same value
     assert np.array_equal(eng.download_paths()[0], srv.download_path(slot))
     acc, att, st = srv.replica_status()
     assert att[slot] == 6 * 32 and st[slot] == 0

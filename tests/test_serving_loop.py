@@ -44,11 +44,11 @@ class FakeServer:
         for v in self.live.values():
             v[1] += v[3]
 
-    def energies(self):
+    def energies(self, slots=None):
         e = np.full(self.slots, np.nan)
         for s, (rid, att, _, _) in self.live.items():
             e[s] = np.sin(rid * 1.3 + att * 0.01)
-        return e
+        return e if slots is None else e[list(slots)]
 
     def download_path(self, s):
         return np.zeros(1)
@@ -91,7 +91,7 @@ def test_admission_by_budget_and_completion():
         ra = r.round_attempts
         assert 1 <= ra <= r.attempts
         assert r.done >= r.attempts and r.done - r.attempts < ra
-        assert len(r.energies) == loop.rounds_for(r)
+        assert len(r.energies) == loop.samples_for(r) >= 1
         assert r.finished >= r.admitted >= r.arrival
 
 
