@@ -249,6 +249,32 @@ def test_largest_node_species_matches_checker(pimc, precision):
     assert np.all(att == n) and np.all(st == 0)
 
 
+@pytest.mark.parametrize("block", [256, 128])
+def test_largest_matrices_at_level_5_match_checker(pimc, block):
+    # 32 + 32 particles, level 5 (the serving mix's largest requests): at 8
+    # warps the Slater scratch lives in global memory, at 4 warps the LU and
+    # inverse fit in shared memory; both reproduce the checker's decisions.
+    from pimc_gb300 import workloads as WL
+    kw = dict(counts=[32, 32], sho_omega=[1.0, 1.0], nslice=128, beta=128 / 25.6, nlevel=5,
+              coulomb=1, norder=3, node_kind=[1, 1], node_omega=[1.0, 1.0],
+              node_temperature=0.25, cell=WL.DOT_CELL)
+    tabs, _ = pimc.coulomb_tables(kw)
+    path = W.initial_path(O.make_config(**kw), "const", seed=43)
+    e = pimc.Engine(kw, 1, tabs, None, seed=6)
+    e.configure(block, 0, 0, 2)
+    e.upload_paths([path])
+    n = 30
+    rec = e.run_sections(n, records=True)
+    port = O.PortOracle(O.make_config(**dict(kw, seed=6, replica=0)), tabs, None)
+    port.set_path(path)
+    pr = port.run(n)
+    assert np.array_equal(pr["reject_level"], rec["reject_level"][0])
+    assert np.array_equal(pr["ipart"], rec["ipart"][0])
+    assert rel_close(pr["ds"], rec["ds"][0][:, :9], 1e-12)
+    assert rel_close(pr["ds_node"], rec["ds_node"][0][:, :9], 1e-6)
+    assert np.abs(port.get_path() - e.download_paths()[0]).max() <= 1e-12
+
+
 def test_graph_steps_equal_direct_calls(pimc):
     # The captured step graph (sweep + energy measurement, replayed) is the same
     # work as the direct calls: energies and paths bit for bit, and a replay
