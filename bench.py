@@ -109,11 +109,11 @@ def sweep_attempts(kw):
 # profiles/fp64_work_per_attempt.md; they are the roofline numerator.
 MEASURED_WORK = {
     # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
-    ("dot20_fn", "mixed"): (2.412e5, 1.194e5),
-    ("dot20_fn", "fp64"): (4.790e5, 1.193e5),
-    ("batch4096", "mixed"): (1.624e5, 3.738e4),   # counted on the first 1024 replicas
-    ("heg54", "mixed"): (3.981e6, 2.041e6),
-    ("dot2", "fp64"): (1.896e4, 622.4),
+    ("dot20_fn", "mixed"): (2.412e5, 1.188e5),
+    ("dot20_fn", "fp64"): (4.790e5, 1.190e5),
+    ("batch4096", "mixed"): (1.624e5, 3.723e4),   # counted on the first 1024 replicas
+    ("heg54", "mixed"): (3.802e6, 2.037e6),
+    ("dot2", "fp64"): (1.896e4, 613.5),
 }
 
 
