@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
   __shared__ long long nacc;
   __shared__ int rnext, flag;
   __shared__ double node_total;
+  __shared__ Smem M_;  // carved pointers, shared so that callees read them from shared memory
   for (;;) {
     if (threadIdx.x == 0) {
       const int k = atomicAdd(P.next, 1);
@@ -68,6 +69,7 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
         dst[i] = src[i];
     }
     if (threadIdx.x == 0) {
+      M_ = carve(smem, P.lay, P.sys[r], P.nodescr_g);
       status = P.state[r].status;
       nacc = 0;
       for (int k = 0; k < kMaxSpecies; ++k) {
@@ -77,7 +79,7 @@ __global__ void __launch_bounds__(kBlock) displace_kernel(DisplaceParams P) {
     }
     __syncthreads();
     const DevSys& s = S;
-    Smem m = carve(smem, P.lay, s, P.nodescr_g);
+    const Smem& m = M_;
     double* path = P.paths + s.path_offset;
     double* cache = (P.nodecache && s.nc_offset >= 0) ? P.nodecache + s.nc_offset : nullptr;
     double* scr = P.scratch + (size_t)blockIdx.x * P.scratch_stride;

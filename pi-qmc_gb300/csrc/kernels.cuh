@@ -749,6 +749,9 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
   __shared__ uint32_t status;
   __shared__ long long nacc;
   __shared__ int rnext;
+  // The carved pointers live in shared memory: the called phases take them
+  // by reference, which would otherwise place them in each thread's stack.
+  __shared__ Smem M_;
   // Persistent CTAs take replicas from a queue ordered longest-first, so that
   // uneven replicas (different N, M, L) balance across the SMs.
   for (;;) {
@@ -766,6 +769,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         dst[i] = src[i];
     }
     if (threadIdx.x == 0) {
+      M_ = carve(smem, P.lay, P.sys[r], P.nodescr_g);
       status = P.state[r].status;
       nacc = 0;
       for (int k = 0; k < kMaxSpecies; ++k) {
@@ -775,7 +779,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
     }
     __syncthreads();
     const DevSys& s = S;
-    Smem m = carve(smem, P.lay, s, P.nodescr_g);
+    const Smem& m = M_;
     double* path = P.paths + s.path_offset;
     const uint32_t att0 = P.state[r].attempt;
     double* cache = (P.nodecache && s.nc_offset >= 0) ? P.nodecache + s.nc_offset : nullptr;
