@@ -845,29 +845,44 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         top_levels(s, m, scale[msp], msp, ipart, lb, L, mynode, cache, ifirst1, P.seed, att, lds,
                    llt, lnd);
         __syncthreads();
-        if (threadIdx.x == 0) {
-          double old = 0.0;
-          for (int level = L; level >= lb; --level) {
-            const double ds = lds[level], dsn = lnd[level], lnT = llt[level];
-            const double total = s.fixed_node ? ds + dsn : ds;
+        if (threadIdx.x < 32) {
+          // Lane i takes level L - i: every level's acceptance probability
+          // exp(lnT - total + total of the level above) and uniform at once
+          // (the same operations as one level after the other); the first
+          // rejecting level from the top decides, and only the levels down to
+          // it count as evaluated.
+          const int lane = threadIdx.x, level = L - lane;
+          const bool mine = level >= lb;
+          double total = 0.0, ds = 0.0, dsn = 0.0, lnT = 0.0;
+          bool rej = false;
+          if (mine) {
+            ds = lds[level];
+            dsn = lnd[level];
+            lnT = llt[level];
+            total = s.fixed_node ? ds + dsn : ds;
+            const double old =
+                level == L ? 0.0 : (s.fixed_node ? lds[level + 1] + lnd[level + 1] : lds[level + 1]);
             const uint32_t ubase = level_uniform_base(s, level);
             const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
             const uint32_t uacc = ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
             const double p = exp(lnT + (-total + old));
             const double u = stream_uniform(P.seed, s.stream_id, att, uacc);
-            if (rec) {
-              rec->ds[level] = ds;
-              rec->ds_node[level] = dsn;
-              rec->lnt[level] = lnT;
-            }
-            if (!(isfinite(lnT) && isfinite(ds))) status |= PIMC_STATUS_NONFINITE;
-            old = total;
-            if (u > p) {
-              m.ictl[C_REJECT] = level;
-              break;
-            }
+            rej = u > p;
           }
-          m.red[kWarps + 2] = old;
+          const unsigned rmask = __ballot_sync(0xffffffffu, rej);
+          const int last = rmask ? __ffs(rmask) - 1 : L - lb;  // lowest evaluated lane's index
+          const bool evaluated = mine && lane <= last;
+          if (evaluated && rec) {
+            rec->ds[level] = ds;
+            rec->ds_node[level] = dsn;
+            rec->lnt[level] = lnT;
+          }
+          const bool bad = evaluated && !(isfinite(lnT) && isfinite(ds));
+          if (__ballot_sync(0xffffffffu, bad) && lane == 0) status |= PIMC_STATUS_NONFINITE;
+          if (lane == last) {
+            if (rmask) m.ictl[C_REJECT] = level;
+            m.red[kWarps + 2] = total;
+          }
         }
         __syncthreads();
         reject = m.ictl[C_REJECT];
