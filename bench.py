@@ -109,7 +109,7 @@ def sweep_attempts(kw):
 # profiles/fp64_work_per_attempt.md; they are the roofline numerator.
 MEASURED_WORK = {
     # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
-    ("dot20_fn", "mixed"): (2.412e5, 1.188e5),
+    ("dot20_fn", "mixed"): (2.412e5, 1.123e5),
     ("dot20_fn", "fp64"): (4.790e5, 1.190e5),
     ("batch4096", "mixed"): (1.624e5, 3.723e4),   # counted on the first 1024 replicas
     ("heg54", "mixed"): (3.802e6, 2.037e6),
