@@ -103,34 +103,35 @@ struct ThermoParams {
   Layout lay;
 };
 
-// True when the minimum image of -v is not the negative of v's (a component
-// exactly at half a box length, where the image rounding breaks the tie
-// one way): the pair term then differs between the two orderings.
-__device__ __forceinline__ bool pbc_tie(const DevSys& s, double x, double y, double z) {
+// The minimum image of the difference v (pbc above) and whether it is a tie:
+// the image of -v is not the negative of v's (a component exactly at half a
+// box length, where the image rounding breaks the tie one way), so the pair
+// term differs between the two orderings.  Both from one product cellb v per
+// component: the image and the tie test share it.
+__device__ __forceinline__ bool pbc_and_tie(const DevSys& s, double& x, double& y, double& z) {
   if (!(dot3(x, y, z, x, y, z) > s.rcut2)) return false;
-  const double v[3] = {x, y, z};
+  double v[3] = {x, y, z};
+  bool tie = false;
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const double ip = floor(__dadd_rn(__dmul_rn(s.cellb[d], v[d]), 1000.5)) - 1000;
-    const double im = floor(__dadd_rn(__dmul_rn(s.cellb[d], -v[d]), 1000.5)) - 1000;
-    if (im != -ip) return true;
+    const double u = __dmul_rn(s.cellb[d], v[d]);
+    const double ip = floor(__dadd_rn(u, 1000.5)) - 1000;
+    const double im = floor(__dadd_rn(-u, 1000.5)) - 1000;
+    tie |= im != -ip;
+    v[d] = __dsub_rn(v[d], __dmul_rn(s.cell[d], ip));
   }
-  return false;
+  x = v[0];
+  y = v[1];
+  z = v[2];
+  return tie;
 }
 
-// utau of the ordered pair (i, j) on the link ending at slice t (PairAction's
-// derivative term of the Coulomb pair action, src/action/PairAction.cc:509-599).
-__device__ double pair_utau_ordered(const DevSys& s, const DevTable& tb, const double* path, int i,
-                                    int j, int t) {
-  const int np = s.npart, M = s.nslice;
-  const int tm = t == 0 ? M - 1 : t - 1;
-  const double* b1 = path + ((size_t)t * np + i) * 3;
-  const double* b0 = path + ((size_t)tm * np + i) * 3;
-  const double* c1 = path + ((size_t)t * np + j) * 3;
-  const double* c0 = path + ((size_t)tm * np + j) * 3;
-  double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
-  pbc(s, ex, ey, ez);
-  double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
-  pbc(s, px, py, pz);
+// utau of a pair from the minimum images e (link end) and p (link start) of
+// its differences (PairAction's derivative term of the Coulomb pair action,
+// src/action/PairAction.cc:509-599).
+__device__ __forceinline__ double pair_utau_images(const DevSys& s, const DevTable& tb, double ex,
+                                                   double ey, double ez, double px, double py,
+                                                   double pz) {
   if (s.mixed) {
     const float fx = (float)ex, fy = (float)ey, fz = (float)ez;
     const float gx = (float)px, gy = (float)py, gz = (float)pz;
@@ -154,7 +155,7 @@ __device__ double pair_utau_ordered(const DevSys& s, const DevTable& tb, const d
 // The pair's share of Σ_links utau: pi-qmc adds 0.5 utau for each ordering
 // (PairAction::getBeadAction runs over every partner of every particle); the two
 // orderings agree unless an image tie makes them differ, so one evaluation
-// usually stands for both.
+// usually stands for both, and the ordering (j, i) is evaluated only on a tie.
 __device__ double pair_utau(const DevSys& s, const DevTable& tb, const double* path, int i, int j,
                             int t) {
   const int np = s.npart, M = s.nslice;
@@ -163,11 +164,17 @@ __device__ double pair_utau(const DevSys& s, const DevTable& tb, const double* p
   const double* b0 = path + ((size_t)tm * np + i) * 3;
   const double* c1 = path + ((size_t)t * np + j) * 3;
   const double* c0 = path + ((size_t)tm * np + j) * 3;
-  const bool tie = pbc_tie(s, b1[0] - c1[0], b1[1] - c1[1], b1[2] - c1[2]) ||
-                   pbc_tie(s, b0[0] - c0[0], b0[1] - c0[1], b0[2] - c0[2]);
-  const double a = pair_utau_ordered(s, tb, path, i, j, t);
-  if (!tie) return a;
-  return 0.5 * a + 0.5 * pair_utau_ordered(s, tb, path, j, i, t);
+  double ex = b1[0] - c1[0], ey = b1[1] - c1[1], ez = b1[2] - c1[2];
+  double px = b0[0] - c0[0], py = b0[1] - c0[1], pz = b0[2] - c0[2];
+  const bool tie1 = pbc_and_tie(s, ex, ey, ez);
+  const bool tie0 = pbc_and_tie(s, px, py, pz);
+  const double a = pair_utau_images(s, tb, ex, ey, ez, px, py, pz);
+  if (!(tie1 || tie0)) return a;
+  double fx = c1[0] - b1[0], fy = c1[1] - b1[1], fz = c1[2] - b1[2];
+  double gx = c0[0] - b0[0], gy = c0[1] - b0[1], gz = c0[2] - b0[2];
+  pbc(s, fx, fy, fz);
+  pbc(s, gx, gy, gz);
+  return 0.5 * a + 0.5 * pair_utau_images(s, tb, fx, fy, fz, gx, gy, gz);
 }
 
 // Pair k of round rd of the round-robin schedule over n (even) players: every
