@@ -114,7 +114,8 @@ enum {
   PIMC_STATUS_INIT_CROSSING = 1,  /* node crossing found when a section was set up */
   PIMC_STATUS_SINGULAR = 2,       /* a Slater matrix had an exactly zero pivot */
   PIMC_STATUS_RESCALE_LIMIT = 4,  /* determinant rescaling hit its iteration limit */
-  PIMC_STATUS_NONFINITE = 8       /* a non-finite bead coordinate was seen */
+  PIMC_STATUS_NONFINITE = 8       /* a non-finite bead coordinate arrived (pimc_upload_paths,
+                                     pimc_server_admit) or a move's action or ln T was not finite */
 };
 
 typedef struct pimc_engine pimc_engine;
@@ -392,7 +393,9 @@ int pimc_node_scale(pimc_engine* e, int replica, int ispec, double* scale);
  * scale is the node model's current scale (pimc_node_scale).  Limits: node
  * species of at most 32 particles, npart <= 1024; larger sizes return
  * PIMC_ERR_CAPACITY.  The first call on a device looks up the scratch array's
- * device address on that device, so make it before any stream capture.  Every
+ * device address on that device, so make it before any stream capture; the
+ * address is kept until exit, so a device reset (cudaDeviceReset) between calls
+ * is not supported.  Every
  * call shares the one scratch array: calls that overlap on the GPU race and
  * must be ordered by the caller (one stream, or events).  Asynchronous.
  * This entry point has no counterpart in the reference. */

@@ -8,6 +8,7 @@ repository, and the output goes only to oracle/_ref/ (git-ignored).  LAPACK
 carry a ``scipy_`` prefix (see oracle/shim/config.h).
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+(default: $PIMC_REFERENCE_TREE, else /root/reference)
 """
 import concurrent.futures as cf
 import glob
@@ -43,6 +44,9 @@ SOURCES = [
     "algorithm/WritePaths.cc", "algorithm/PathReader.cc",
 ]
 
+# where the reference tree lies (read-only); the environment variable overrides
+DEFAULT_TREE = os.environ.get("PIMC_REFERENCE_TREE", "/root/reference")
+
 FLAGS = ["-std=gnu++98", "-O2", "-fPIC", "-w", "-ffp-contract=off", "-DHAVE_CONFIG_H"]
 
 
@@ -55,7 +59,7 @@ def openblas():
     return os.path.abspath(libs[0])
 
 
-def build(ref_root="/root/reference", verbose=False):
+def build(ref_root=DEFAULT_TREE, verbose=False):
     src = os.path.join(ref_root, "src")
     if not os.path.isdir(src):
         raise FileNotFoundError(f"reference tree not found at {ref_root}")
@@ -88,4 +92,4 @@ def build(ref_root="/root/reference", verbose=False):
 
 
 if __name__ == "__main__":
-    build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", verbose=True)
+    build(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_TREE, verbose=True)

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -891,6 +892,13 @@ int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (e->server) return fail(PIMC_ERR_INVALID, "a server takes paths at admission");
   CU(cudaMemcpyAsync(e->d_paths.p, host_xyz, e->path_off[e->nrep] * sizeof(double),
                      cudaMemcpyHostToDevice, e->stream));
+  {
+    const dim3 grid(16, (unsigned)std::min(e->nrep, 65535));
+    path_scan_kernel<<<grid, kBlock, 0, e->stream>>>(e->d_sys.p, e->d_state.p, e->d_paths.p,
+                                                     e->nrep);
+    CU(cudaGetLastError());
+    e->launches++;
+  }
   if (e->d_nodecache.p) {  // new paths: every cached Slater result is rebuilt
     CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double), e->stream));
     if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep)) return rc;
@@ -1866,6 +1874,11 @@ int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_ta
   DevState st;
   memset(&st, 0, sizeof(st));
   for (int k = 0; k < kMaxSpecies; ++k) st.node_scale[k] = 1.0;
+  for (long long i = 0; i < pw; ++i)  // the admission's counterpart of path_scan_kernel
+    if (!std::isfinite(host_path[i])) {
+      st.status |= PIMC_STATUS_NONFINITE;
+      break;
+    }
   CU(cudaMemcpyAsync(e->d_sys.p + r, &e->hsys[r], sizeof(DevSys), cudaMemcpyHostToDevice,
                      e->stream));
   CU(cudaMemcpyAsync(e->d_state.p + r, &st, sizeof(DevState), cudaMemcpyHostToDevice, e->stream));
@@ -2024,10 +2037,14 @@ int pimc_server_pool(pimc_engine* e, size_t* used, size_t* largest_free) {
 
 // Allocation-free node evaluation.  The device address of the static scratch
 // array is looked up once per device (cudaGetSymbolAddress, with that device
-// current) on the first call made on it, and cached.
+// current) on the first call made on it, and cached in an atomic slot per
+// device, so host threads calling concurrently see either no address or the
+// whole one (two first calls racing both look it up and store the same value).
+// The cache outlives a context: after cudaDeviceReset the address is stale, and
+// resetting a device between calls is not supported.
 namespace {
 constexpr int kMaxDevices = 64;
-double* g_noalloc_addr[kMaxDevices] = {nullptr};
+std::atomic<double*> g_noalloc_addr[kMaxDevices];
 }  // namespace
 
 int pimc_node_evaluate_noalloc(const pimc_system* sys, int ispec, double scale, int nbatch,
@@ -2043,10 +2060,12 @@ int pimc_node_evaluate_noalloc(const pimc_system* sys, int ispec, double scale, 
   int dev = 0;
   CU(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(PIMC_ERR_CAPACITY, "device ordinal beyond 63");
-  if (!g_noalloc_addr[dev]) {
+  double* scratch = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
     void* p = nullptr;
     CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_addr[dev] = (double*)p;
+    scratch = (double*)p;
+    g_noalloc_addr[dev].store(scratch, std::memory_order_release);
   }
   NoAllocParams P;
   fill_sys(*sys, P.sys);
@@ -2059,7 +2078,7 @@ int pimc_node_evaluate_noalloc(const pimc_system* sys, int ispec, double scale, 
   P.scale = scale;
   P.ispec = ispec;
   P.nbatch = nbatch;
-  P.scratch = g_noalloc_addr[dev];
+  P.scratch = scratch;
   const int grid = nbatch < kNoAllocSlots ? nbatch : kNoAllocSlots;
   const size_t smem = 6 * (size_t)sys->npart * sizeof(double);
   if (smem > 48 * 1024) return fail(PIMC_ERR_CAPACITY, "npart beyond 1024");

@@ -10,6 +10,27 @@
 
 namespace pimc {
 
+// Newly arrived paths are scanned for non-finite coordinates: a replica holding
+// one gets PIMC_STATUS_NONFINITE at upload, before any move reads the bead
+// (pi-qmc has no such check; a NaN would propagate through its actions
+// silently).  Block (x, y) scans a 1/gridDim.x share of the paths of replicas
+// y, y + gridDim.y, ...  The replica's moves still run: every table index and
+// lane choice in the kernels stays in bounds for non-finite inputs (float to
+// int conversions of NaN give 0, pivot searches pick among the group's own
+// lanes), so the status word is the whole effect on the other replicas.
+__global__ void __launch_bounds__(kBlock) path_scan_kernel(const DevSys* sys, DevState* state,
+                                                           const double* paths, int nrep) {
+  for (int r = blockIdx.y; r < nrep; r += gridDim.y) {
+    const long long n = 3LL * sys[r].nslice * sys[r].npart;
+    const double* p = paths + sys[r].path_offset;
+    int bad = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+      bad |= !isfinite(p[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&state[r].status, (uint32_t)PIMC_STATUS_NONFINITE);
+  }
+}
+
 struct PrefillParams {
   const DevSys* sys;
   const DevState* state;

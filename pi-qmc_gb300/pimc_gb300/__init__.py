@@ -20,6 +20,8 @@ PIMC_NODES_NONE, PIMC_NODES_SHO, PIMC_NODES_FREE = 0, 1, 2
 PIMC_MOVER_FREE, PIMC_MOVER_FREE_PBC = 0, 1
 PIMC_PREC_FP64, PIMC_PREC_MIXED = 0, 1
 PIMC_ERR_INVALID, PIMC_ERR_CUDA, PIMC_ERR_NO_DEVICE, PIMC_ERR_CAPACITY = -1, -2, -3, -4
+PIMC_STATUS_INIT_CROSSING, PIMC_STATUS_SINGULAR = 1, 2
+PIMC_STATUS_RESCALE_LIMIT, PIMC_STATUS_NONFINITE = 4, 8
 STATUS_BITS = {1: "init_crossing", 2: "singular", 4: "rescale_limit", 8: "nonfinite"}
 
 

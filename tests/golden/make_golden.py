@@ -12,12 +12,19 @@ estimator together with the Ewald table and short-range grid it built), and
 for some cases a recorded run of rigid-displacement moves from the final path
 (DisplaceMoveSampler / DoubleDisplaceMoveSampler with a UniformMover).  For two
 cases the final path is also written by pi-qmc's WritePaths (<case>.paths) and
-read back by its PathReader (path_files.npz).
+read back by its PathReader (path_files.npz).  For the fixed-node cases of
+workloads.NODE_CASES, nodes_<case>.npz holds pi-qmc's NodeModel::evaluate and
+evaluateDistance (SHONodes, FreeParticleNodes) on seeded slice pairs near the
+final path, at the scale the node model reached; for the ill-conditioned SHO dot
+(omega/T = 20) it also holds the same determinants and distances evaluated in
+60-digit arithmetic (mpmath) from the same double inputs, the exact values the
+FP64 implementations are measured against.
 
 The fixtures let machines without the reference tree (the GPU machine) pin the C++
 restatement and the CUDA engine against the reference's own outputs.
 
-Usage: python tests/golden/make_golden.py   (needs the reference tree)
+Usage: python tests/golden/make_golden.py [case ...]   (needs the reference tree;
+no case names: every case)
 """
 import os
 import sys
@@ -141,11 +148,89 @@ def make_path_files():
     print("path files:", ", ".join(k[:-5] for k in out if k.endswith("_read")))
 
 
-def main():
+NODE_PAIRS = 24
+EXACT_DIGITS = 60
+
+
+def sho_exact(r1, r2, ifirst, n, omega, temperature, mass, tau, scale):
+    """SHONodes' determinant and nodal distances (src/fixednode/SHONodes.cc:51-170)
+    in EXACT_DIGITS-digit arithmetic from the double inputs: the matrix
+    scale exp(-c((r_i^2 + r_j^2) cosh - 2 r_i.r_j)), its determinant, and
+    d = sqrt(2m / ((|sum_i inv(j,i) scale grad_ij|^2 + 1e-15) tau)) for both sides."""
+    import mpmath as mp
+    mp.mp.dps = EXACT_DIGITS
+    wt = mp.mpf(omega) * mp.mpf(0.5) / mp.mpf(temperature)
+    ch, c = mp.cosh(wt), mp.mpf(mass) * mp.mpf(0.5) * mp.mpf(omega) / mp.sinh(wt)
+    S = mp.mpf(scale)
+    R1 = [[mp.mpf(float(x)) for x in r1[ifirst + j]] for j in range(n)]
+    R2 = [[mp.mpf(float(x)) for x in r2[ifirst + i]] for i in range(n)]
+    dot = lambda a, b: a[0] * b[0] + a[1] * b[1] + a[2] * b[2]  # noqa: E731
+    E = [[mp.exp(-c * ((dot(R2[i], R2[i]) + dot(R1[j], R1[j])) * ch - 2 * dot(R2[i], R1[j])))
+          for j in range(n)] for i in range(n)]
+    A = mp.matrix([[S * E[i][j] for j in range(n)] for i in range(n)])
+    det = mp.det(A)
+    X = A ** -1
+    k = 2 * mp.mpf(mass) / mp.mpf(tau)
+
+    def dist(g):
+        return float(mp.sqrt(k / (g[0] ** 2 + g[1] ** 2 + g[2] ** 2 + mp.mpf(1e-15))))
+
+    d1 = [dist([sum(X[j, i] * S * 2 * c * (R2[i][d] - ch * R1[j][d]) * E[i][j]
+                    for i in range(n)) for d in range(3)]) for j in range(n)]
+    d2 = [dist([sum(X[j, i] * S * 2 * c * (R1[j][d] - ch * R2[i][d]) * E[i][j]
+                    for j in range(n)) for d in range(3)]) for i in range(n)]
+    return float(det), np.array(d1), np.array(d2)
+
+
+def make_node_fixture(name):
+    """pi-qmc's node models on NODE_PAIRS seeded slice pairs (slice t and t + M/2 of
+    the final golden path, each coordinate moved by N(0, 0.05^2)), every node
+    species, islice 0, at the scale pi-qmc's own set-up rescaling reached."""
+    kw, init, n = W.GOLDEN_CASES[name]
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    ref.set_path(W.initial_path(cfg, init))
+    ref.run(n)
+    x1 = ref.get_path()
+    M, npart = cfg.nslice, cfg.npart
+    rng = np.random.default_rng(4242)
+    ts = rng.integers(0, M // 2, NODE_PAIRS)
+    r1 = x1[ts] + 0.05 * rng.normal(size=(NODE_PAIRS, npart, 3))
+    r2 = x1[ts + M // 2] + 0.05 * rng.normal(size=(NODE_PAIRS, npart, 3))
+    out = dict(config=np.array(repr(kw)), r1=r1, r2=r2)
+    firsts = np.cumsum([0] + [cfg.spec_count[i] for i in range(cfg.nspecies)])
+    for sp in range(cfg.nspecies):
+        if not cfg.node_kind[sp]:
+            continue
+        res = [ref.node_eval(sp, r1[b], r2[b], 0, False) for b in range(NODE_PAIRS)]
+        out[f"sp{sp}_scale"] = np.array(ref.node_scale(sp))
+        out[f"sp{sp}_err"] = np.array([r[0] for r in res], np.int32)
+        out[f"sp{sp}_det"] = np.array([r[1] for r in res])
+        out[f"sp{sp}_d1"] = np.array([r[2] for r in res])
+        out[f"sp{sp}_d2"] = np.array([r[3] for r in res])
+        if name == "dot20_fn":
+            ex = [sho_exact(r1[b], r2[b], firsts[sp], cfg.spec_count[sp], cfg.node_omega[sp],
+                            cfg.node_temperature, cfg.spec_mass[sp], cfg.tau,
+                            ref.node_scale(sp)) for b in range(NODE_PAIRS)]
+            out[f"sp{sp}_exact_det"] = np.array([e[0] for e in ex])
+            out[f"sp{sp}_exact_d1"] = np.array([e[1] for e in ex])
+            out[f"sp{sp}_exact_d2"] = np.array([e[2] for e in ex])
+            out[f"sp{sp}_first"] = np.array(firsts[sp])
+    path = os.path.join(HERE, "nodes_" + name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"nodes_{name}: {NODE_PAIRS} slice pairs, {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main(names=()):
     for name, (kw, init, n) in W.GOLDEN_CASES.items():
-        run_case(name, kw, init, n)
-    make_path_files()
+        if not names or name in names:
+            run_case(name, kw, init, n)
+    for name in W.NODE_CASES:
+        if not names or name in names or ("nodes_" + name) in names:
+            make_node_fixture(name)
+    if not names or "path_files" in names:
+        make_path_files()
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -51,3 +51,23 @@ def load(name):
                 path1=z["path0"] + z["dpath"], energy0=float(z["energy0"]),
                 energy1=float(z["energy1"]), records=rec, nattempt=int(z["nattempt"]),
                 naccepted=int(z["naccepted"]))
+
+
+def load_nodes(name):
+    """NodeModel fixture of a case: slice pairs r1, r2 [nb][npart][3] and, per
+    node species sp, pi-qmc's scale, err, det, d1, d2 (and for the SHO dot at
+    omega/T = 20 the 60-digit values exact_det, exact_d1, exact_d2 over the
+    species' own particles, which start at index `first`)."""
+    z = np.load(os.path.join(GOLDEN, "nodes_" + name + ".npz"))
+    kw = ast.literal_eval(str(z["config"]))
+    out = dict(kw=kw, r1=z["r1"], r2=z["r2"], species={})
+    for sp in range(len(kw["counts"])):
+        if f"sp{sp}_det" not in z:
+            continue
+        d = {k: z[f"sp{sp}_{k}"] for k in ("err", "det", "d1", "d2")}
+        d["scale"] = float(z[f"sp{sp}_scale"])
+        if f"sp{sp}_exact_det" in z:
+            d.update(exact_det=z[f"sp{sp}_exact_det"], exact_d1=z[f"sp{sp}_exact_d1"],
+                     exact_d2=z[f"sp{sp}_exact_d2"], first=int(z[f"sp{sp}_first"]))
+        out["species"][sp] = d
+    return out

@@ -7,7 +7,7 @@ import subprocess
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("PIMC_REFERENCE_TREE", "/root/reference")
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),

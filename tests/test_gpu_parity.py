@@ -7,9 +7,10 @@ itself pinned to the reference by tests/test_oracle.py.
 Tolerances: plain action differences and mover ratios 1e-12 relative (to
 max(|value|, 1)); section-move decisions (section start, particle, rejecting
 level) exact; paths 1e-12; node-model terms 1e-10 relative, except the
-omega/T = 20 SHO dot whose Slater matrices have condition numbers ~1e9 (see
-tests/test_oracle.py), held to 1e-2 relative on the nodal action with exact
-decisions.
+omega/T = 20 SHO dot whose Slater matrices have condition numbers 1e12 - 3e13:
+there every FP64 implementation (pi-qmc's, the restatement, this engine) is
+held to 2e-3 relative of the 60-digit values and of each other (the study is in
+tests/test_oracle.py), with exact decisions.
 """
 import numpy as np
 import pytest
@@ -20,7 +21,8 @@ import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-NODE_TOL = {"dot20_fn": 1e-2}
+NODE_TOL = {"dot20_fn": 2e-3}
+EXACT_TOL = 2e-3
 
 
 def rel_close(a, b, tol, floor=1.0):
@@ -101,7 +103,7 @@ def test_second_launch_continues_the_chain(pimc):
     assert np.array_equal(a.download_paths()[0], b.download_paths()[0])
 
 
-@pytest.mark.parametrize("case", ["dot2_small", "heg8"])
+@pytest.mark.parametrize("case", ["dot2_small", "heg8", "dot3_prim"])
 def test_action_difference_every_level(pimc, case):
     g = golden_io.load(case)
     cfg = O.make_config(**g["kw"])
@@ -140,6 +142,54 @@ def test_node_evaluate(pimc, case):
             assert abs(det[b] - pdet) <= 1e-10 * abs(pdet)
             assert rel_close(d1[b], pd1, 1e-10)
             assert rel_close(d2[b], pd2, 1e-10)
+
+
+@pytest.mark.parametrize("case", list(W.NODE_CASES))
+def test_node_models_match_golden(pimc, case):
+    # The engine's SHONodes / FreeParticleNodes (pimc_node_evaluate) on pi-qmc's
+    # own NodeModel::evaluate + evaluateDistance outputs: same slice pairs, the
+    # scale pi-qmc's set-up reached; the ill-conditioned dot also against the
+    # 60-digit values of the same inputs.
+    z = golden_io.load_nodes(case)
+    g = golden_io.load(case)
+    cfg = O.make_config(**z["kw"])
+    e = engine_for(pimc, g)
+    st = e.replica_state(0)
+    for sp, ref in z["species"].items():
+        st["node_scale"][sp] = ref["scale"]
+    e.set_replica_state(0, st)
+    tol = NODE_TOL.get(case, 1e-10)
+    for sp, ref in z["species"].items():
+        err, det, d1, d2 = e.node_evaluate(sp, z["r1"], z["r2"])
+        assert np.array_equal(err, ref["err"])
+        assert np.all(np.abs(det - ref["det"]) <= tol * np.abs(ref["det"])), sp
+        assert rel_close(d1, ref["d1"], tol, floor=0.0), sp
+        assert rel_close(d2, ref["d2"], tol, floor=0.0), sp
+        if "exact_det" in ref:
+            f, n = ref["first"], cfg.spec_count[sp]
+            assert np.all(np.abs(det - ref["exact_det"]) <= EXACT_TOL * np.abs(ref["exact_det"]))
+            assert rel_close(d1[:, f:f + n], ref["exact_d1"], EXACT_TOL, floor=0.0)
+            assert rel_close(d2[:, f:f + n], ref["exact_d2"], EXACT_TOL, floor=0.0)
+
+
+def test_ill_conditioned_dot_matches_checker(pimc):
+    # The headline fixed-node dot (N=20, SHONodes, M=1024, L=5) run by the engine
+    # and by the restatement from the same path and streams: decisions exact,
+    # plain action differences 1e-12, node terms within the conditioning bar.
+    g = golden_io.load("dot20_fn")
+    cfg = O.make_config(**g["kw"])
+    e = engine_for(pimc, g)
+    e.upload_paths([g["path1"]])
+    rec = e.run_sections(60, records=True)
+    port = O.PortOracle(cfg, g["tables"], g["ewald"])
+    port.set_path(g["path1"])
+    pr = port.run(60)
+    for k in ("ifirst1", "ifirst2", "ipart", "reject_level"):
+        assert np.array_equal(rec[k][0], pr[k]), k
+    nl = g["kw"]["nlevel"] + 1
+    assert rel_close(rec["ds"][0][:, :nl], pr["ds"][:, :nl], 1e-12)
+    assert rel_close(rec["ds_node"][0][:, :nl], pr["ds_node"][:, :nl], NODE_TOL["dot20_fn"])
+    assert np.abs(e.download_paths()[0] - port.get_path()).max() <= 1e-12
 
 
 def test_thermo_energy_matches_checker(pimc):

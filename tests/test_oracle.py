@@ -11,11 +11,17 @@ import oracle_lib as O
 import workloads as W
 
 # Tolerances.  Plain action differences and mover ratios: 1e-12 relative.
-# Node-model differences: 1e-10 relative for well-conditioned Slater matrices;
-# dot20_fn (omega/T = 20) has Slater matrices with condition numbers ~1e9, where
-# two correct LU orderings (OpenBLAS vs this one) differ at ~1e-3 relative in the
-# nodal action, so that case is held to 1e-2 relative and exact decisions.
-NODE_TOL = {"dot20_fn": 1e-2}
+# Node-model differences: 1e-10 relative for well-conditioned Slater matrices.
+# dot20_fn (SHONodes at omega/T = 20) is the exception: its 10x10 Slater
+# matrices have 1-norm condition numbers of 1e12 - 3e13 (tests/golden/nodes_dot20_fn.npz,
+# computed in 60-digit arithmetic), and rounding the matrix elements to FP64
+# alone, before any factorisation, moves the determinant by up to 3e-5.  Against
+# the 60-digit values of the same double inputs, pi-qmc (OpenBLAS dgetrf/dgetri)
+# lands within 1.1e-3 and this restatement within 9e-4 on determinants and
+# nodal distances, and the two differ from each other by up to 6e-4.  That case
+# is held to 2e-3 relative on node values and nodal action, with exact decisions.
+NODE_TOL = {"dot20_fn": 2e-3}
+EXACT_TOL = 2e-3   # FP64 against the 60-digit values, for the ill-conditioned dot
 
 
 def rel_close(a, b, tol, floor=1.0):
@@ -202,3 +208,48 @@ def test_port_displace_matches_golden(case):
     assert np.allclose(r["ds"], ref["ds"], rtol=1e-12, atol=1e-12)
     assert np.allclose(r["ds_node"], ref["ds_node"], rtol=1e-10, atol=1e-10)
     assert np.abs(port.get_path() - d["path"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("case", list(W.NODE_CASES))
+def test_port_node_models_match_golden(case):
+    # SHONodes / FreeParticleNodes of the restatement on pi-qmc's own
+    # NodeModel::evaluate + evaluateDistance outputs (same slice pairs, same
+    # scale): determinant, error flag and both distance arrays.  For the
+    # ill-conditioned dot both are also held to the 60-digit values.
+    z = golden_io.load_nodes(case)
+    g = golden_io.load(case)
+    cfg = O.make_config(**z["kw"])
+    port = O.PortOracle(cfg, g["tables"], g["ewald"])
+    tol = NODE_TOL.get(case, 1e-12)
+    nb = len(z["r1"])
+    assert z["species"], case
+    for sp, ref in z["species"].items():
+        O.PortOracle.lib().port_set_node_scale(port.h, sp, ref["scale"])
+        for b in range(nb):
+            err, det, d1, d2 = port.node_eval(sp, z["r1"][b], z["r2"][b], 0, False)
+            assert err == ref["err"][b]
+            assert abs(det - ref["det"][b]) <= tol * abs(ref["det"][b]), (sp, b)
+            assert rel_close(d1, ref["d1"][b], tol, floor=0.0), (sp, b)
+            assert rel_close(d2, ref["d2"][b], tol, floor=0.0), (sp, b)
+            if "exact_det" in ref:
+                f, n = ref["first"], cfg.spec_count[sp]
+                for got in (det, ref["det"][b]):
+                    assert abs(got - ref["exact_det"][b]) <= EXACT_TOL * abs(ref["exact_det"][b])
+                for got, ex in ((d1, ref["exact_d1"][b]), (d2, ref["exact_d2"][b]),
+                                (ref["d1"][b], ref["exact_d1"][b]),
+                                (ref["d2"][b], ref["exact_d2"][b])):
+                    assert rel_close(got[f:f + n], ex, EXACT_TOL, floor=0.0), (sp, b)
+
+
+def test_node_fixtures_exercise_the_nodal_action():
+    # The periodic golden cases are not vacuous: pi-qmc's records of the warm
+    # electron gas hold nonzero free-particle nodal actions and node crossings
+    # (2e100), and the other cases' dot and gas node terms are nonzero too.
+    g = golden_io.load("heg16_hot")
+    dsn = g["records"]["ds_node"][:, :g["kw"]["nlevel"] + 1]
+    assert np.sum((dsn != 0) & (dsn < 1e99)) > 500
+    assert np.sum(dsn >= 1e99) >= 3
+    for case in W.NODE_CASES:
+        for ref in golden_io.load_nodes(case)["species"].values():
+            assert np.all(ref["det"] != 0) and np.all(np.isfinite(ref["d1"]))
+            assert np.any(ref["d1"] < 200) and np.any(ref["d2"] < 200)

@@ -15,4 +15,17 @@ GOLDEN_CASES = {
     "dot20_fn": (dot20_fn(), "const", 40),
     "heg8": (heg54(n=8, nslice=128, nlevel=3), "grid", 150),
     "heg54": (heg54(), "grid", 12),
+    # a warmer, coarser electron gas (16 electrons, T/T_F = 1, M = 32): nodal
+    # distances of a few tau-lengths, so the free-particle nodal action is
+    # nonzero on most attempts and moves cross the nodes now and then
+    "heg16_hot": (heg54(n=16, nslice=32, nlevel=3, t_over_tf=1.0), "grid", 800),
+    # primitive confinement a r^2 + b r^4 (PrimSHOAction) with a Coulomb pair
+    # action, no harmonic action, on three electrons of two species
+    "dot3_prim": (dot2(counts=[2, 1], sho_omega=[0.0, 0.0], prim_a=[0.5, 0.3],
+                       prim_b=[0.05, 0.1], nslice=64, nlevel=3, beta=4.0), "gauss", 500),
 }
+
+# NodeModel fixtures (tests/golden/nodes_<case>.npz): pi-qmc's own
+# NodeModel::evaluate + evaluateDistance on seeded slice pairs near the final
+# golden path of these cases
+NODE_CASES = ("dot4_fn", "dot20_fn", "heg8", "heg54", "heg16_hot")
