@@ -19,6 +19,7 @@ workload on all host cores (the C++ restatement of pi-qmc's code when the
 reference build is not present on the machine).
 """
 import argparse
+import hashlib
 import json
 import math
 import multiprocessing as mp
@@ -53,7 +54,12 @@ def parse():
     p.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
                    help="auto: the precision the workload is specified in (FP64 for dot2, "
                         "FP32 bulk + FP64 determinants for the others)")
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="timed seconds of the engine line's all-core CPU baseline")
+    p.add_argument("--equil", type=int, default=-1,
+                   help="untimed equilibration steps before the warm-up (-1: per workload)")
+    p.add_argument("--serve-requests", type=int, default=600,
+                   help="requests of the serving sub-run in the default line (0: none)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     p.add_argument("--requests", type=int, default=2000, help="serve: requests in the stream")
@@ -102,18 +108,19 @@ def sweep_attempts(kw):
 
 
 # ------------------------------------------------------- measured work per unit
-# Thread-level FP64 flops (DADD + DMUL + 2 DFMA, predicated-on lanes only) and
-# DRAM bytes (read + write) per section attempt of the section kernel, counted
-# by ncu on the same kernel and workload after a warm-up step (the timed step of
-# a bench run).  The commands and raw counts are in
-# profiles/fp64_work_per_attempt.md; they are the roofline numerator.
+# Thread-level FP64 flops (DADD + DMUL + 2 DFMA), FP32 flops (FADD + FMUL +
+# 2 FFMA), predicated-on lanes only, and DRAM bytes (read + write) per section
+# attempt of the section kernel, counted by ncu on the same kernel and workload
+# after a warm-up step.  `sha` is kernel_source_sha() of the build they were
+# counted on: another build's counts are not used (the line then falls back to
+# the operation-count model and says so).
 MEASURED_WORK = {
-    # (workload, precision): (FP64 flops per attempt, DRAM bytes per attempt or None)
-    ("dot20_fn", "mixed"): (2.412e5, 1.123e5),
-    ("dot20_fn", "fp64"): (4.790e5, 1.190e5),
-    ("batch4096", "mixed"): (1.624e5, 3.723e4),   # counted on the first 1024 replicas
-    ("heg54", "mixed"): (3.802e6, 2.037e6),
-    ("dot2", "fp64"): (1.896e4, 613.5),
+    ("dot20_fn", "mixed"): dict(fp64=2.412e5, fp32=None, dram=1.123e5, sha="292ad9418616be78"),
+    ("dot20_fn", "fp64"): dict(fp64=4.790e5, fp32=None, dram=1.190e5, sha="292ad9418616be78"),
+    # counted on the first 1024 replicas of the mix
+    ("batch4096", "mixed"): dict(fp64=1.624e5, fp32=None, dram=3.723e4, sha="292ad9418616be78"),
+    ("heg54", "mixed"): dict(fp64=3.802e6, fp32=None, dram=2.037e6, sha="292ad9418616be78"),
+    ("dot2", "fp64"): dict(fp64=1.896e4, fp32=None, dram=613.5, sha="292ad9418616be78"),
 }
 
 
@@ -220,31 +227,55 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU side
+# The CPU implementation of the path: pi-qmc's own hot-path code (oracle/_ref)
+# where the reference tree was built on this machine, else the C++
+# restatement (oracle/liboracle_port.so).  It loads nothing from the engine:
+# pi-qmc builds its own tables, and the restatement takes the tables pi-qmc
+# built for these workloads from the golden fixtures.
+def reference_tables(kw):
+    """pi-qmc's pair tables (and Ewald table) for a bench workload's system."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import golden_io
+    import workloads as TW
+    for name, (gkw, _, _) in TW.GOLDEN_CASES.items():
+        if gkw == kw:
+            g = golden_io.load(name)
+            return g["tables"], g["ewald"]
+    mix = golden_io.load_tables("dot_mix")
+    base = mix["kw"]
+    same = all(kw.get(k, 1.0) == base.get(k, 1.0) for k in ("masses", "charges", "cell"))
+    if same and abs(kw["beta"] / kw["nslice"] - base["beta"] / base["nslice"]) < 1e-15:
+        return WL.tables_for(kw, mix["tables"]), None
+    raise KeyError("no pi-qmc tables recorded for this system")
+
+
 def _cpu_worker(args):
-    kw, seed, replica, seconds, attempts = args
+    kw, seed, replica, warmup, steps, chunk = args
     # pi-qmc's constructors print progress to stdout; keep the JSON line clean
     devnull = os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    sys.path.insert(0, os.path.join(REPO, "pi-qmc_gb300"))
     import oracle_lib as O
-    import pimc_gb300
-    tabs, ew = pimc_gb300.coulomb_tables(kw)
     cfg = O.make_config(**dict(kw, seed=seed, replica=replica))
     if O.RefOracle.available():
         sim = O.RefOracle(cfg)
     else:
+        tabs, ew = reference_tables(kw)
         sim = O.PortOracle(cfg, tabs, ew)
     sim.set_path(WL.initial_path(cfg, init_kind_for(kw), seed=seed + replica))
-    # pi-qmc's loop body: a sweep of section moves, then one energy measurement
-    chunk = attempts or sweep_attempts(kw)
-    n, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
+    # pi-qmc's loop body: `chunk` section attempts, then one energy measurement
+    n = 0
+    for _ in range(warmup):
+        sim.run(chunk, first_attempt=n)
+        sim.thermo_energy()
+        n += chunk
+    t0 = time.perf_counter()
+    for _ in range(steps):
         sim.run(chunk, first_attempt=n)
         sim.thermo_energy()
         n += chunk
     dt = time.perf_counter() - t0
-    return n * ((1 << kw["nlevel"]) - 1), n, dt
+    return steps * chunk * ((1 << kw["nlevel"]) - 1), steps * chunk, dt
 
 
 def init_kind_for(kw):
@@ -253,23 +284,62 @@ def init_kind_for(kw):
     return "const" if any(kw.get("node_kind", [0])) else "gauss"
 
 
-def cpu_throughput(kws, seconds, cores, attempts=0):
-    """Bead-updates/s of the CPU implementation on `cores` processes (process p
-    runs replica p of the workload)."""
+def cpu_throughput(kws, steps, warmup, cores, chunk):
+    """Bead-updates/s of the CPU implementation on `cores` processes: process p
+    runs replica p of the workload through `warmup` untimed and `steps` timed
+    steps of `chunk` attempts each.  Returns (value, attempts, timed wall of
+    the slowest process)."""
     kws = kws if isinstance(kws, list) else [kws]
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(kws[r % len(kws)], 777, r, seconds, attempts)
+        res = pool.map(_cpu_worker, [(kws[r % len(kws)], 777, r, warmup, steps,
+                                      chunk or sweep_attempts(kws[r % len(kws)]))
                                      for r in range(cores)])
     beads = sum(b for b, _, _ in res)
     wall = max(dt for _, _, dt in res)
-    return beads / wall, sum(n for _, n, _ in res)
+    return beads / wall, sum(n for _, n, _ in res), wall
 
 
 def cpu_kind():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_lib as O
     return "reference" if O.RefOracle.available() else "port"
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_baseline(kws, chunk, seconds, cores):
+    """The CPU implementation on all host cores, one process per replica stream,
+    sized to about `seconds` of timed work, plus one process alone (the
+    single-core rate).  Returns the cpu_baseline record."""
+    one, _, w1 = cpu_throughput(kws, 1, 0, 1, chunk)  # one step alone: its length
+    steps = max(1, int(round(seconds / max(w1, 1e-3))))
+    single, _, _ = cpu_throughput(kws, max(1, steps // 2), 1, 1, chunk)
+    value, attempts, wall = cpu_throughput(kws, steps, 1, cores, chunk)
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": cpu_kind(),
+            "cpu_model": cpu_model(), "single_core_value": single,
+            "all_core_per_core_value": value / cores,
+            "sample": f"{cores} processes (one replica each, replicas 0..{cores - 1} of the "
+                      f"workload), each 1 untimed and {steps} timed steps of "
+                      f"{chunk or 'one sweep of'} section attempts + one energy "
+                      f"measurement; {attempts} timed attempts in {wall:.1f} s"}
 
 
 # ---------------------------------------------------------------- serving arm
@@ -362,13 +432,21 @@ def run_serve(args, rank, world):
 
 
 # ---------------------------------------------------------------- engine arm
-def run_engine(args, rank, world):
-    import torch
-    import pimc_gb300
-    if args.workload == "serve":
-        return run_serve(args, rank, world)
+def bench_config(args, R, A, batch, kw, path_bytes):
+    """The `config` record, the same for both arms: the workload and one step."""
+    L = kw["nlevel"]
+    return {"workload": f"{args.workload}: " + describe(args.workload),
+            "step": "one sweep of section moves per replica + one thermodynamic "
+                    "energy measurement per replica",
+            "replicas_per_gpu": R, "attempts_per_replica_per_step": A,
+            "bead_updates_per_attempt": (1 << L) - 1 if not batch else "2^L-1 per replica",
+            "precision": args.precision,
+            "l2": "paths (%.0f MB) exceed L2 and a 256 MB buffer is written between steps"
+                  % (path_bytes / 1e6),
+            "parallelism": f"replicas{args.gpus}"}
 
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+
+def engine_setup(args):
     kws = workload_kw(args.workload)
     batch = isinstance(kws, list)
     if batch and args.replicas:
@@ -377,6 +455,32 @@ def run_engine(args, rank, world):
     R = len(kws) if batch else (args.replicas or R0)
     kw = kws[0] if batch else kws
     A = args.attempts or A0 or sweep_attempts(kw)
+    return kws, batch, R, kw, A
+
+
+def energy_stats(E, what):
+    """Mean thermodynamic energy of measurements E [steps][replicas] and its
+    standard error from the per-replica means (each replica an independent
+    chain: one block per replica)."""
+    E = np.asarray(E, float)
+    per = E.mean(axis=0)
+    ok = np.isfinite(per)
+    v = per[ok]
+    err = float(v.std(ddof=1) / math.sqrt(len(v))) if len(v) > 1 else None
+    return {"value": float(v.mean()) if len(v) else None, "stat_err": err,
+            "blocks": int(ok.sum()), "measurements": int(E.size),
+            "unit": "Hartree (reduced units)", "when": what,
+            "sigma": "standard error of the per-replica means (independent chains as blocks)"}
+
+
+def run_engine(args, rank, world):
+    import torch
+    import pimc_gb300
+    if args.workload == "serve":
+        return run_serve(args, rank, world)
+
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    kws, batch, R, kw, A = engine_setup(args)
     prec = pimc_gb300.PIMC_PREC_MIXED if args.precision == "mixed" else pimc_gb300.PIMC_PREC_FP64
     seed = rank_seed(rank)
     if batch:
@@ -400,18 +504,20 @@ def run_engine(args, rank, world):
 
     paths = np.concatenate([WL.initial_path(shape_of(systems[r]), init_kind(args.workload),
                                             seed=100 + r).ravel() for r in range(R)])
-    host = torch.from_numpy(paths).pin_memory()
     eng.upload_paths(paths)
     # launch configuration chosen by the autotuner (untimed; the chains are restored)
     tuned, tried = eng.autotune(min(A, 32)) if not args.no_autotune else (eng.launch_config(), [])
     # depth statistics for the flop model (untimed)
     rec = eng.run_sections(4, records=True)
-    # fraction of attempts that evaluate each level, by depth below the top level
     Ls = np.array([k["nlevel"] for k in systems])[:, None]
     rl = rec["reject_level"]
     depth_reach = [float(np.mean((rl < 0) | (rl <= Ls - d))) for d in range(int(Ls.max()) + 1)]
     reach = [depth_reach[L - lev] for lev in range(L + 1)]
     eng.upload_paths(paths)
+    # equilibration (untimed): the energy block below is taken on equilibrated chains
+    equil = args.equil if args.equil >= 0 else default_equil(args.workload)
+    if equil:
+        eng.run_steps(A, equil, energies=False)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         eng.run_steps(A, 1, energies=False)
@@ -421,57 +527,41 @@ def run_engine(args, rank, world):
     n_launch0 = eng.kernel_launches
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
+    E = np.empty((args.steps, R))
     with ClockSampler() as clk:
         torch.cuda.synchronize()
         for i in range(args.steps):
             flush.fill_(float(i))
             ev[i][0].record(stream)
-            eng.run_steps(A, 1, energies=False)  # one captured graph: sweep + measurement
+            # one captured graph (sweep + measurement); the step's energies to the host
+            E[i] = eng.run_steps(A, 1, energies=True)[0]
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     launches = eng.kernel_launches - n_launch0
-    energy = eng.thermo_energy()  # energies after the last step (untimed re-measurement)
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    t_ms = sum(step_ms)
-    t_ms = max_over_ranks(t_ms, world)
+    t_ms = max_over_ranks(sum(step_ms), world)
     units = A * sum((1 << k["nlevel"]) - 1 for k in systems)
     value = world * units * args.steps / (t_ms * 1e-3)
-    # ---- end to end through the public API, host buffers each step
+    energy_block = energy_stats(E, f"the {args.steps} timed steps, after {equil} equilibration "
+                                   f"and {args.warmup} warm-up steps from the initial paths")
+    energy_block.update(energy_vs_reference(args.workload, energy_block, equil + args.warmup))
+    # ---- end to end through the public API: each step uploads the chain's
+    # current paths from pinned host memory, runs the sweep, measures, and
+    # brings the energies and the paths back (the next step's input)
     e2e_steps = max(2, min(args.steps, 5))
+    host = torch.empty(paths.size, dtype=torch.float64).pin_memory().numpy()
+    eng.download_paths(out=host)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        eng.upload_paths(host.numpy())
+        eng.upload_paths(host)
         eng.run_sections(A)
         e2e_energy = eng.thermo_energy()
+        eng.download_paths(out=host)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = world * units * e2e_steps / e2e_s
-    # ---- energy against the FP64 form (same seeds, paths and step count)
     assert np.all(np.isfinite(e2e_energy))
-    energy_block = energy_stats(energy)
-    if args.precision == "mixed":
-        if batch:
-            ref = pimc_gb300.Engine.batch(kws, [WL.tables_for(k, base) for k in kws], seed=seed)
-        else:
-            ref = pimc_gb300.Engine(kw, R, tabs, ew, seed=seed)
-        ref.set_stream(stream.cuda_stream)
-        ref.configure(tuned["block"], tuned["scratch_global"], tuned["ctas_per_sm"],
-                      tuned["regs_variant"])
-        ref.upload_paths(paths)          # the same history as the measured engine:
-        ref.run_sections(4)              # depth-statistics attempts, re-upload,
-        ref.upload_paths(paths)          # warm-up and timed steps
-        for _ in range(args.warmup + args.steps):
-            ref.run_steps(A, 1, energies=False)
-        e64 = energy_stats(ref.thermo_energy())
-        ref.close()
-        energy_block["fp64"] = e64
-        diff = energy_block["value"] - e64["value"]
-        energy_block["diff_vs_fp64"] = diff
-        sig = math.hypot(e64["stat_err"] or 0.0, energy_block["stat_err"] or 0.0)
-        energy_block["diff_over_sigma"] = diff / sig if sig else None
-        energy_block["within_2sigma_of_fp64"] = bool(abs(diff) <= 2 * sig)
-        energy_block["sigma"] = "combined: sqrt(stat_err^2 + fp64 stat_err^2)"
     # ---- the plain form: one replica, FP64, same sweep (untimed by the step loop)
     plain = None if batch else pimc_gb300.Engine(kw, 1, tabs, ew, seed=seed)
     plain_value = None
@@ -499,52 +589,24 @@ def run_engine(args, rank, world):
         a1.record(stream)
     torch.cuda.synchronize()
     section_ms = statistics.mean(a0.elapsed_time(a1) for a0, a1 in sec_ev)
-    fp64_peak = pimc_gb300.fp64_peak_tflops()
-    work = MEASURED_WORK.get((args.workload, args.precision))
-    if work is not None:
-        flops = work[0] * R * A
-        traffic = work[1] * R * A if work[1] is not None else None
-        flops_source = ("ncu thread-level DADD+DMUL+2*DFMA per attempt of this kernel and "
-                        "workload (profiles/fp64_work_per_attempt.md) x attempts per launch")
-    else:
-        if batch:
-            flops = sum(attempt_flops(k, [depth_reach[k["nlevel"] - lev]
-                                          for lev in range(k["nlevel"] + 1)])
-                        for k in systems) * A
-        else:
-            flops = attempt_flops(kw, reach) * R * A
-        traffic = None
-        flops_source = "operation-count model (bench.py attempt_flops); no ncu count yet"
-    achieved = flops / (section_ms * 1e-3) / 1e12
+    roofline = section_roofline(args, systems, batch, kw, R, A, reach, depth_reach, section_ms,
+                                pimc_gb300)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded initial paths; Philox4x32-10 proposals)",
-        "config": {"workload": f"{args.workload}: " + describe(args.workload),
-                   "step": "one sweep of section moves per replica + one thermodynamic "
-                           "energy measurement per replica",
-                   "replicas_per_gpu": R, "attempts_per_replica_per_step": A,
-                   "bead_updates_per_attempt": (1 << L) - 1 if not batch else "2^L-1 per replica",
-                   "precision": args.precision,
-                   "l2": "paths (%.0f MB) exceed L2 and a 256 MB buffer is written between steps"
-                         % (paths.nbytes / 1e6),
-                   "parallelism": f"replicas{world}",
-                   "launch": {"chosen": tuned, "candidates": tried}},
+        "config": bench_config(args, R, A, batch, kw, paths.nbytes),
+        "launch": {"chosen": tuned, "candidates": tried},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(paths.nbytes),
-                "d2h_bytes_per_step": int(R * 8),
-                "path": "pimc_upload_paths (pinned host) + pimc_run_sections + pimc_thermo_energy"},
+                "d2h_bytes_per_step": int(paths.nbytes + R * 8),
+                "steps": e2e_steps,
+                "path": "per step: pimc_upload_paths (the chain's current paths, pinned host) + "
+                        "pimc_run_sections + pimc_thermo_energy + pimc_download_paths (pinned "
+                        "host, the next step's input); the chain continues from the timed steps"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                     "section_ms_per_launch": section_ms, "flops_per_launch": flops,
-                     "flops_source": flops_source,
-                     "peak_source": "measured FP64 FMA probe (pimc_fp64_peak); "
-                                    "MEASURED_PEAKS.json holds no FP64 figure",
-                     "traffic": traffic, "kernel": "section_moves_kernel",
-                     "flops_per_attempt_model": attempt_flops(kw, reach),
-                     "level_reach": reach},
+        "roofline": roofline,
         "clocks": clk.summary(),
         "energy": energy_block,
     }
@@ -556,16 +618,118 @@ def run_engine(args, rank, world):
     return out
 
 
-def energy_stats(e):
-    """Mean thermodynamic energy over replicas and its standard error (replicas
-    are independent chains)."""
-    e = np.asarray(e, float)
-    ok = np.isfinite(e)
-    v = e[ok]
-    err = float(v.std(ddof=1) / math.sqrt(len(v))) if len(v) > 1 else None
-    return {"value": float(v.mean()) if len(v) else None, "stat_err": err,
-            "replicas": int(ok.sum()), "unit": "Hartree (reduced units)",
-            "when": "after the warm-up and timed steps"}
+def default_equil(name):
+    # untimed sweeps before the warm-up: the chains of the dots start from
+    # constant-in-time (or per-slice Gaussian) paths
+    return {"dot20_fn": 100, "dot2": 200, "heg54": 0, "batch4096": 0, "serve": 0}[name]
+
+
+# equilibrated energies of pi-qmc's own code (tests/golden/make_energy.py) for
+# the bench workloads that have one
+REFERENCE_ENERGY = {"dot20_fn": "dot20_fn", "dot2": "dot2_full"}
+
+
+def energy_vs_reference(name, block, equil_steps):
+    """The bench's energy against pi-qmc's FP64 energy of the same system:
+    |E - E_pi-qmc| <= 2 sqrt(sigma^2 + sigma_pi-qmc^2)."""
+    case = REFERENCE_ENERGY.get(name)
+    f = os.path.join(REPO, "tests", "golden", f"energy_{case}.npz") if case else None
+    if not f or not os.path.exists(f):
+        return {"reference": None}
+    z = np.load(f)
+    er, sr = float(z["energy"]), float(z["sigma"])
+    sig = math.hypot(sr, block["stat_err"] or 0.0)
+    d = block["value"] - er
+    return {"reference": {"value": er, "stat_err": sr, "blocks": int(z["block_means"].size),
+                          "what": f"pi-qmc's own code (FP64), {int(z['block_means'].shape[0])} "
+                                  f"chains after {int(z['equil'])} sweeps, blocks of "
+                                  f"{int(z['block'])} sweeps"},
+            "diff_vs_reference": d, "diff_over_sigma": d / sig if sig else None,
+            "within_2sigma_of_reference": bool(abs(d) <= 2 * sig),
+            "relative_stat_err": (block["stat_err"] or 0.0) / abs(block["value"]),
+            "equilibration_sweeps": equil_steps}
+
+
+def kernel_source_sha():
+    """Digest of the section kernel's sources: the counted work per attempt
+    below belongs to the kernel these files build."""
+    d = os.path.join(REPO, "pi-qmc_gb300", "csrc")
+    h = hashlib.sha256()
+    for f in ("section_kernel.cuh", "kernels.cuh", "pimc_device.cuh", "pimc_rng.h",
+              "section_variants.cu"):
+        h.update(f.encode())
+        h.update(open(os.path.join(d, f), "rb").read())
+    return h.hexdigest()[:16]
+
+
+def section_roofline(args, systems, batch, kw, R, A, reach, depth_reach, section_ms, pimc_gb300):
+    """FP64- and FP32-pipe rooflines of the section kernel: counted work per
+    attempt x attempts per launch / the kernel's CUDA-event time, over the
+    measured FMA peaks of this device."""
+    fp64_peak = pimc_gb300.fp64_peak_tflops()
+    fp32_peak = pimc_gb300.fp32_peak_tflops()
+    work = MEASURED_WORK.get((args.workload, args.precision))
+    sha = kernel_source_sha()
+    stale = work is not None and work["sha"] != sha
+    if work is not None and not stale:
+        flops = work["fp64"] * R * A
+        flops32 = work["fp32"] * R * A if work.get("fp32") is not None else None
+        traffic = work["dram"] * R * A if work.get("dram") is not None else None
+        source = ("ncu thread-level DADD+DMUL+2*DFMA (FP64) and FADD+FMUL+2*FFMA (FP32) per "
+                  "attempt of this kernel build and workload x attempts per launch")
+    else:
+        if batch:
+            flops = sum(attempt_flops(k, [depth_reach[k["nlevel"] - lev]
+                                          for lev in range(k["nlevel"] + 1)])
+                        for k in systems) * A
+        else:
+            flops = attempt_flops(kw, reach) * R * A
+        flops32 = traffic = None
+        source = ("operation-count model (attempt_flops): "
+                  + ("the counted work belongs to another build of the kernel"
+                     if stale else "no hardware count for this workload"))
+    achieved = flops / (section_ms * 1e-3) / 1e12
+    out = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+           "frac": achieved / fp64_peak, "traffic": traffic, "kernel": "section_moves_kernel",
+           "section_ms_per_launch": section_ms, "flops_per_launch": flops,
+           "flops_source": source, "count_stale": stale, "kernel_sha": sha,
+           "peak_source": "measured FP64 FMA probe (pimc_fp64_peak); MEASURED_PEAKS.json holds "
+                          "no FP64 figure",
+           "flops_per_attempt_model": attempt_flops(kw, reach), "level_reach": reach}
+    if flops32 is not None:
+        a32 = flops32 / (section_ms * 1e-3) / 1e12
+        out["fp32"] = {"achieved": a32, "peak": fp32_peak, "unit": "TFLOP/s",
+                       "frac": a32 / fp32_peak,
+                       "peak_source": "measured FP32 FMA probe (pimc_fp32_peak)"}
+    return out
+
+
+# ---------------------------------------------------------------- serving sub-run
+def serving_subrun(args):
+    """A short run of the serving stream (config 5's distributions and arrival
+    rate) carried in the default line: p50/p99 time-to-result."""
+    sub = argparse.Namespace(**vars(args))
+    sub.workload = "serve"
+    sub.requests = args.serve_requests
+    sub.warmup = 1
+    sub.precision = "mixed"
+    out = run_serve(sub, 0, 1)
+    return {"value": out["value"], "unit": UNIT, "latency": out["latency"],
+            "requests": sub.requests, "rate_per_s": sub.rate, "sweep_scale": sub.sweep_scale,
+            "rounds": out["steps"], "wall_s": out["ms_per_step"] * out["steps"] / 1e3,
+            "gpu_launches": out["gpu_launches"],
+            "admitted_while_others_ran": out["admitted_while_others_ran"],
+            "offered_bead_updates_per_s": out["config"]["offered_bead_updates_per_s"],
+            "workload": describe("serve"),
+            "scaling_note": SERVE_SCALING_NOTE}
+
+
+SERVE_SCALING_NOTE = (
+    "config 5 asks 1e3..1e5 sweeps per request; a request is one Markov chain whose section "
+    "attempts depend on each other, and the largest (N=64, M=2048, 1e5 sweeps) is 4e8 "
+    "dependent attempts, days of one chain on any device, so no stream of these requests "
+    "completes in a bench run at any arrival rate.  The stream keeps config 5's arrival "
+    "rate and size distributions and scales every request's sweeps by sweep_scale.")
 
 
 def describe(name):
@@ -586,44 +750,54 @@ def describe(name):
     }[name]
 
 
+def run_reference(args, world):
+    """The reference arm: pi-qmc's CPU implementation of the same workload on
+    all host cores (one process per replica stream; --steps timed steps after
+    --warmup untimed ones, each the engine arm's step: A section attempts and
+    one energy measurement per replica).  Loads no engine code."""
+    kws, batch, R, kw, A = engine_setup(args)
+    cores = os.cpu_count() or 1
+    value, attempts, wall = cpu_throughput(kws, args.steps, args.warmup, cores, A)
+    path_bytes = sum(3 * 8 * k["nslice"] * sum(k["counts"])
+                     for k in (kws if batch else [kw] * R))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded initial paths; Philox4x32-10 proposals)",
+            "config": bench_config(args, R, A, batch, kw, path_bytes),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": cpu_kind(),
+                             "cpu_model": cpu_model(), "all_core_per_core_value": value / cores,
+                             "sample": f"{cores} processes, one replica each (replicas "
+                                       f"0..{cores - 1} of the workload), each {args.warmup} "
+                                       f"untimed and {args.steps} timed steps of {A} section "
+                                       f"attempts + one energy measurement; {attempts} timed "
+                                       f"attempts, slowest process {wall:.2f} s"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse()
     args.precision = workload_precision(args.workload, args.precision)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    args.gpus = world
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "engine" else "gloo")
     if args.impl == "reference":
         if rank == 0:
-            kw = workload_kw(args.workload)
-            cores = os.cpu_count() or 1
-            t0 = time.perf_counter()
-            value, attempts = cpu_throughput(kw, max(2.0, args.cpu_seconds / 2), cores,
-                                             defaults(args.workload)[1])
-            wall = time.perf_counter() - t0
-            kind = cpu_kind()
-            out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-                   "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                   "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
-                   "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                   "config": {"workload": f"{args.workload}: " + describe(args.workload)},
-                   "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                                    "sample": f"{attempts} section attempts over {cores} "
-                                              f"processes, one replica each"},
-                   "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                           "d2h_bytes_per_step": 0}}
-            print(json.dumps(out))
+            print(json.dumps(run_reference(args, world)))
         return
     out = run_engine(args, rank, world)
-    if rank == 0:
+    if rank == 0 and world == 1:
+        if args.workload != "serve" and args.serve_requests > 0:
+            out["serving"] = serving_subrun(args)
         if not args.no_cpu_baseline:
-            kw = workload_kw(args.workload)
-            cores = os.cpu_count() or 1
-            v, att = cpu_throughput(kw, args.cpu_seconds, cores, defaults(args.workload)[1])
-            out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": cpu_kind(),
-                                   "sample": f"{att} section attempts of the same workload "
-                                             f"over {cores} processes ({args.cpu_seconds:.0f} s)"}
+            kws, batch, R, kw, A = engine_setup(args)
+            out["cpu_baseline"] = cpu_baseline(kws, A, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

@@ -417,6 +417,8 @@ int pimc_stream_sample(uint64_t seed, uint32_t replica, uint32_t attempt, int n,
 /* Measured dense FP64 FMA throughput of the current device in TFLOP/s (a
  * short probe kernel; the roofline denominator for the FP64-bound kernels). */
 int pimc_fp64_peak(double* tflops);
+/* The same for FP32 FMAs (the denominator of the mixed form's FP32 work). */
+int pimc_fp32_peak(double* tflops);
 
 /* Kernel launches issued by this engine so far (for launch accounting). */
 int64_t pimc_kernel_launches(pimc_engine* e);

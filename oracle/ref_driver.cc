@@ -355,6 +355,37 @@ extern "C" void* ref_create(const ora_config* c) {
   return s;
 }
 
+// Hooks for the pi-qmc-side adapters test: the composite action, or one
+// species' node model inside its FixedNodeAction, replaced by another object of
+// the same pi-qmc interface, so that pi-qmc's own samplers, section choosers
+// and FixedNodeAction run on it.  `action` is an Action*, `model` a NodeModel*.
+extern "C" void ref_replace_action(void* h, void* action) {
+  RefSim* s = (RefSim*)h;
+  s->rec->inner = (Action*)action;
+}
+
+extern "C" int ref_replace_node_model(void* h, int ispec, void* model) {
+  RefSim* s = (RefSim*)h;
+  if (!s->dcomposite || ispec < 0 || ispec >= (int)s->nodes.size() || !s->nodes[ispec]) return -1;
+  int first = 0;
+  for (int i = 0; i < ispec; ++i) first += s->cfg.spec_count[i];
+  for (size_t k = 0; k < s->dcomposite->actions.size(); ++k) {
+    FixedNodeAction* f = dynamic_cast<FixedNodeAction*>(s->dcomposite->actions[k]);
+    if (f && f->ifirst == first) {
+      f->nodeModel = (NodeModel*)model;
+      f->matrixUpdateObj = 0;
+      s->nodes[ispec] = (NodeModel*)model;
+      return 0;
+    }
+  }
+  return -1;
+}
+
+// The SerialPaths object (a Paths&) and the SimulationInfo of a simulation,
+// for adapters that take them.
+extern "C" void* ref_paths(void* h) { return (Paths*)((RefSim*)h)->paths; }
+extern "C" void* ref_simulation_info(void* h) { return ((RefSim*)h)->simInfo; }
+
 extern "C" void ref_destroy(void* h) {
   // The reference objects hold cross references without clear ownership; the
   // checker process is short-lived, so they are left for process exit.

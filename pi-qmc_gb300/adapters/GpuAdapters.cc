@@ -1,5 +1,6 @@
 #include "GpuAdapters.h"
 
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -42,36 +43,96 @@ double GpuCompositeAction::getActionDifference(const SectionSamplerInterface& sa
 
 void GpuCompositeAction::getBeadAction(const Paths&, int, int, double&, double&, double&, Vec&,
                                        Vec&) const {
-  throw std::runtime_error("GpuCompositeAction: per-bead actions run in gpuThermoEnergy");
+  throw std::logic_error(
+      "GpuCompositeAction::getBeadAction: per-bead actions are summed on the device "
+      "(gpuThermoEnergy, pimc_virial_energy)");
 }
 
-GpuNodeModel::GpuNodeModel(pimc_engine* engine, int ispec, int npart)
-    : NodeModel("_gpu"), engine(engine), ispec(ispec), npart(npart),
-      r1buf(3 * npart), r2buf(3 * npart), d1buf(npart), d2buf(npart) {}
+GpuNodeModel::GpuNodeModel(pimc_engine* engine, int ispec, int npart, int count, int maxlevel)
+    : NodeModel("_gpu"), engine(engine), ispec(ispec), npart(npart), count(count), scale(1.0),
+      slices((1 << maxlevel) + 1), r1buf(3 * npart), r2buf(3 * npart) {
+  for (size_t k = 0; k < slices.size(); ++k) slices[k].valid = false;
+  pushScale();
+}
 
-NodeModel::DetWithFlag GpuNodeModel::evaluate(const VArray& r1, const VArray& r2, const int,
-                                              bool) {
+// The engine evaluates at its replica-0 scale for the species: keep it this model's.
+void GpuNodeModel::pushScale() {
+  pimc_replica_state st;
+  check(pimc_get_replica_state(engine, 0, &st), "pimc_get_replica_state");
+  if (st.node_scale[ispec] == scale) return;
+  st.node_scale[ispec] = scale;
+  check(pimc_set_replica_state(engine, 0, &st), "pimc_set_replica_state");
+}
+
+void GpuNodeModel::pack(const VArray& r1, const VArray& r2) {
   for (int i = 0; i < npart; ++i)
     for (int d = 0; d < 3; ++d) {
       r1buf[3 * i + d] = r1(i)[d];
       r2buf[3 * i + d] = r2(i)[d];
     }
+}
+
+GpuNodeModel::SliceResult& GpuNodeModel::slot(int islice) {
+  if (islice < 0) throw std::out_of_range("GpuNodeModel: negative slice index");
+  if (islice >= (int)slices.size()) {
+    const size_t old = slices.size();
+    slices.resize(islice + 1);
+    for (size_t k = old; k < slices.size(); ++k) slices[k].valid = false;
+  }
+  return slices[islice];
+}
+
+// One evaluation of the packed positions at the current scale, kept for islice.
+NodeModel::DetWithFlag GpuNodeModel::evaluateOnce(int islice) {
+  SliceResult& r = slot(islice);
+  r.d1.resize(npart);
+  r.d2.resize(npart);
   DetWithFlag res;
   int err = 0;
-  check(pimc_node_evaluate(engine, ispec, 1, &r1buf[0], &r2buf[0], &res.det, &d1buf[0],
-                           &d2buf[0], &err),
+  check(pimc_node_evaluate(engine, ispec, 1, &r1buf[0], &r2buf[0], &res.det, &r.d1[0],
+                           &r.d2[0], &err),
         "pimc_node_evaluate");
   res.err = err != 0;
+  r.det = res.det;
+  r.r1 = r1buf;
+  r.r2 = r2buf;
+  r.valid = true;
   return res;
 }
 
-void GpuNodeModel::evaluateDistance(const VArray&, const VArray&, const int, Array& d1,
-                                    Array& d2) {
-  // Distances of the slice pair passed to the preceding evaluate().
-  for (int i = 0; i < npart; ++i) {
-    d1(i) = d1buf[i];
-    d2(i) = d2buf[i];
+NodeModel::DetWithFlag GpuNodeModel::evaluate(const VArray& r1, const VArray& r2,
+                                              const int islice, bool scaleMagnitude) {
+  pack(r1, r2);
+  DetWithFlag res = evaluateOnce(islice);
+  // SHONodes::evaluate's rescale loop (src/fixednode/SHONodes.cc:53-126)
+  for (int guard = 0; scaleMagnitude && !res.err &&
+                      (std::fabs(res.det) < 1e-50 || std::fabs(res.det) > 1e50);
+       ++guard) {
+    if (guard >= 2000) throw std::runtime_error("GpuNodeModel: rescale loop did not converge");
+    if (std::fabs(res.det) < 1e-250)
+      scale *= 2;
+    else
+      scale *= std::pow(std::fabs(res.det), -1. / count);
+    pushScale();
+    res = evaluateOnce(islice);
   }
+  return res;
+}
+
+void GpuNodeModel::evaluateDistance(const VArray& r1, const VArray& r2, const int islice,
+                                    Array& d1, Array& d2) {
+  pack(r1, r2);
+  SliceResult& r = slot(islice);
+  if (!r.valid || r.r1 != r1buf || r.r2 != r2buf) evaluateOnce(islice);
+  for (int i = 0; i < npart; ++i) {
+    d1(i) = r.d1[i];
+    d2(i) = r.d2[i];
+  }
+}
+
+void GpuNodeModel::evaluateGradLogDist(const VArray&, const VArray&, const int, VMatrix&,
+                                       VMatrix&, const Array&, const Array&) {
+  throw std::logic_error("GpuNodeModel::evaluateGradLogDist is not offloaded");
 }
 
 GpuSectionSampler::GpuSectionSampler(Paths& paths, pimc_engine* engine, int attempts)

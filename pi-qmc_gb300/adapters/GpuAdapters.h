@@ -40,8 +40,13 @@ class GpuCompositeAction : public Action {
  public:
   GpuCompositeAction(pimc_engine* engine, int npart, int nlevel);
   virtual double getActionDifference(const SectionSamplerInterface&, int level);
+  // Every action this one replaces returns 0 here (SpringAction.cc:108-110,
+  // SHOAction.cc:67-69, PrimSHOAction.cc:60-63, CoulombAction.cc:150-152,
+  // PairAction.cc:505-507 in src/action), so their composite does too.
   virtual double getTotalAction(const Paths&, const int level) const { return 0; }
-  // Per-bead actions are not offloaded one bead at a time; use gpuThermoEnergy.
+  // Per-bead actions are not offloaded one bead at a time: the estimators'
+  // sums over links run on the device (gpuThermoEnergy, pimc_virial_energy).
+  // A call throws std::logic_error rather than returning wrong values.
   virtual void getBeadAction(const Paths&, int ipart, int islice, double& u, double& utau,
                              double& ulambda, Vec& fm, Vec& fp) const;
 
@@ -52,22 +57,48 @@ class GpuCompositeAction : public Action {
 };
 
 // NodeModel offload for one species (NodeModel::evaluate / evaluateDistance,
-// src/fixednode/NodeModel.h:74-90).  The engine's current scale for the
-// species is used; set-up rescaling happens in GpuSectionSampler.
+// src/fixednode/NodeModel.h:74-90), holding what SHONodes / FreeParticleNodes
+// hold per section slice (src/fixednode/SHONodes.cc:51-170): evaluate(r1, r2,
+// islice) keeps that slice's determinant and nodal distances, and
+// evaluateDistance(r1, r2, islice) returns them when r1, r2 are the positions
+// last evaluated on islice (FixedNodeAction's order: every slice is evaluated
+// at its level before the level-0 distances, src/fixednode/FixedNodeAction.cc:58-100),
+// else evaluates those positions.  The model's scale starts at 1 and follows
+// pi-qmc's rescale loop when evaluate is asked to scale the magnitude
+// (|det| outside [1e-50, 1e50]: scale *= 2 below 1e-250, else |det|^(-1/n));
+// the engine's replica-0 scale for the species is kept equal to it, so the
+// device builds scale * rho exactly as pi-qmc does.  A singular matrix with
+// scaleMagnitude returns err = true instead of pi-qmc's retry-until-exit.
 class GpuNodeModel : public NodeModel {
  public:
-  GpuNodeModel(pimc_engine* engine, int ispec, int npart);
+  // npart: all particles; count: the species' particles (SHONodes' npart);
+  // maxlevel: the bisection level (slices 0 .. 2^maxlevel kept, as SHONodes).
+  GpuNodeModel(pimc_engine* engine, int ispec, int npart, int count, int maxlevel);
   virtual DetWithFlag evaluate(const VArray& r1, const VArray& r2, const int islice,
                                bool scaleMagnitude);
   virtual void evaluateDistance(const VArray& r1, const VArray& r2, const int islice,
                                 Array& d1, Array& d2);
+  // Not offloaded; pi-qmc's FixedNodeAction does not call it (SHONodes' own is
+  // empty).  A call throws std::logic_error.
   virtual void evaluateGradLogDist(const VArray&, const VArray&, const int, VMatrix&,
-                                   VMatrix&, const Array&, const Array&) {}
+                                   VMatrix&, const Array&, const Array&);
+  double getScale() const { return scale; }
 
  private:
+  struct SliceResult {
+    bool valid;
+    double det;
+    std::vector<double> r1, r2, d1, d2;
+  };
   pimc_engine* engine;
-  int ispec, npart;
-  std::vector<double> r1buf, r2buf, d1buf, d2buf;
+  int ispec, npart, count;
+  double scale;
+  std::vector<SliceResult> slices;
+  std::vector<double> r1buf, r2buf;
+  void pack(const VArray& r1, const VArray& r2);
+  SliceResult& slot(int islice);
+  DetWithFlag evaluateOnce(int islice);
+  void pushScale();
 };
 
 // Sampler offload: each run() performs `attempts` section-move attempts of

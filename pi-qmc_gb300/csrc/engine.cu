@@ -215,10 +215,14 @@ int validate(const pimc_system& s) {
   if (tot != s.npart) return fail(PIMC_ERR_INVALID, "species counts do not add up to npart");
   if (s.nlevel < 1 || s.nlevel > PIMC_MAX_LEVEL)
     return fail(PIMC_ERR_CAPACITY, "nlevel must be in 1..6");
-  if (s.nslice < (1 << s.nlevel) + 1) return fail(PIMC_ERR_INVALID, "nslice smaller than a section");
   if (!(s.tau > 0)) return fail(PIMC_ERR_INVALID, "tau must be positive");
   bool fixed = false;
   for (int i = 0; i < s.nspecies; ++i) fixed |= s.node_kind[i] != 0;
+  // A section of 2^nlevel + 1 slices may span the whole ring (nslice = 2^nlevel,
+  // both ends the same bead, as SectionChooser allows); with fixed nodes the
+  // two sections of a double move must each fit.
+  if (s.nslice < (1 << s.nlevel) + (fixed ? 1 : 0))
+    return fail(PIMC_ERR_INVALID, "nslice smaller than a section");
   if (fixed && (s.nslice % 2)) return fail(PIMC_ERR_INVALID, "fixed node needs an even nslice");
   if (fixed && !(s.node_temperature > 0))
     return fail(PIMC_ERR_INVALID, "fixed node needs node_temperature > 0");
@@ -1478,6 +1482,34 @@ int pimc_fp64_peak(double* tflops) {
   for (int rep = 0; rep < 5; ++rep) {
     CU(cudaEventRecord(a));
     fp64_probe_kernel<<<blocks, threads>>>(d, iters);
+    CU(cudaEventRecord(b));
+    CU(cudaEventSynchronize(b));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return PIMC_OK;
+}
+
+int pimc_fp32_peak(double* tflops) {
+  if (!tflops) return fail(PIMC_ERR_INVALID, "null argument");
+  int nsm = 0;
+  if (int rc = device_check(nsm)) return rc;
+  float* d = nullptr;
+  CU(cudaMalloc(&d, sizeof(float)));
+  const int iters = 16384, blocks = nsm * 8, threads = 256;
+  fp32_probe_kernel<<<blocks, threads>>>(d, 16);
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    CU(cudaEventRecord(a));
+    fp32_probe_kernel<<<blocks, threads>>>(d, iters);
     CU(cudaEventRecord(b));
     CU(cudaEventSynchronize(b));
     float ms = 0;

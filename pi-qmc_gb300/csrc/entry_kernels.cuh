@@ -670,6 +670,18 @@ __global__ void fp64_probe_kernel(double* out, int iters) {
   if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5) out[0] = a0;
 }
 
+// The FP32 counterpart: eight independent FMA chains per thread.
+__global__ void fp32_probe_kernel(float* out, int iters) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+  float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+  const float b = 0.9999999f, c = 1e-9f;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+    a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+  }
+  if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5f) out[0] = a0;
+}
+
 __global__ void stream_sample_kernel(uint64_t seed, uint32_t rep, uint32_t att, int n, double* u,
                                      double* z) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

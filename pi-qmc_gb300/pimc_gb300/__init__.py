@@ -170,6 +170,7 @@ def lib():
         L.pimc_node_scale.argtypes = [P, I, I, D]
         L.pimc_stream_sample.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, I, D, D]
         L.pimc_fp64_peak.argtypes = [D]
+        L.pimc_fp32_peak.argtypes = [D]
         L.pimc_node_evaluate_noalloc.argtypes = [C.POINTER(System), I, C.c_double, I, P, P, P,
                                                  P, P, P, P]
         L.pimc_engine_configure.argtypes = [P, C.POINTER(LaunchConfig)]
@@ -288,6 +289,13 @@ def fp64_peak_tflops():
     return v.value
 
 
+def fp32_peak_tflops():
+    """Measured dense FP32 FMA throughput of the device (TFLOP/s)."""
+    v = C.c_double()
+    _check(lib().pimc_fp32_peak(C.byref(v)))
+    return v.value
+
+
 def stream_sample(seed, replica, attempt, n):
     """The first n uniforms and normals of one attempt's streams, generated on
     the GPU (for bit-exact comparison with a CPU replay)."""
@@ -373,8 +381,12 @@ class Engine(_Checkpoint):
         _check(lib().pimc_upload_paths(self.h, _dp(flat)))
         self._last_upload = flat
 
-    def download_paths(self, flat=False):
-        out = np.empty(int(self.offsets[-1]))
+    def download_paths(self, flat=False, out=None):
+        """All replicas' paths; out (a flat float64 array, e.g. a pinned host
+        buffer's view) receives them when given."""
+        if out is None:
+            out = np.empty(int(self.offsets[-1]))
+        assert out.dtype == np.float64 and out.size == self.offsets[-1] and out.flags.c_contiguous
         _check(lib().pimc_download_paths(self.h, _dp(out)))
         if flat:
             return out

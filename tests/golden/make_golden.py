@@ -221,6 +221,30 @@ def make_node_fixture(name):
     print(f"nodes_{name}: {NODE_PAIRS} slice pairs, {os.path.getsize(path) / 1024:.0f} KiB")
 
 
+def make_table_fixture():
+    """tables_dot_mix.npz: the pair tables pi-qmc's CoulombAction builds for the
+    harmonic-dot mixes (batched replicas, serving stream): tau = 1/25.6, unit
+    masses and charges, two species of more than one particle each (pairs
+    (0,0), (0,1), (1,1)), the dot cell.  Every replica of those mixes shares
+    these tables (their tau, masses and charges are the same)."""
+    from pimc_gb300 import workloads as WL
+    kw = dict(WL.batch_dots(1)[0], counts=[2, 2], node_kind=[1, 1], node_omega=[1.0, 1.0],
+              sho_omega=[1.0, 1.0])
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    tabs = ref.pair_tables()
+    out = dict(config=np.array(repr(kw)), npair=len(tabs))
+    for k, t in enumerate(tabs):
+        s1, s2 = O.species_pair_of(t, cfg)
+        out[f"pair{k}_species"] = np.array([s1, s2], np.int32)
+        out[f"pair{k}_grid"] = np.array([t["ngpts"], t["norder"]], np.int32)
+        out[f"pair{k}_params"] = np.array([t["rgridinv"], t["logrratioinv"]])
+        out[f"pair{k}_ugrid"] = t["ugrid"]
+    path = os.path.join(HERE, "tables_dot_mix.npz")
+    np.savez_compressed(path, **out)
+    print(f"tables_dot_mix: {len(tabs)} pair tables, {os.path.getsize(path) / 1024:.0f} KiB")
+
+
 def main(names=()):
     for name, (kw, init, n) in W.GOLDEN_CASES.items():
         if not names or name in names:
@@ -230,6 +254,8 @@ def main(names=()):
             make_node_fixture(name)
     if not names or "path_files" in names:
         make_path_files()
+    if not names or "tables" in names:
+        make_table_fixture()
 
 
 if __name__ == "__main__":

@@ -7,9 +7,7 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def load(name):
-    z = np.load(os.path.join(GOLDEN, name + ".npz"))
-    kw = ast.literal_eval(str(z["config"]))
+def _pair_tables(z):
     tabs = []
     for k in range(int(z["npair"])):
         g = z[f"pair{k}_grid"]
@@ -17,6 +15,19 @@ def load(name):
         tabs.append(dict(species=tuple(int(v) for v in z[f"pair{k}_species"]),
                          ngpts=int(g[0]), norder=int(g[1]), rgridinv=float(p[0]),
                          logrratioinv=float(p[1]), ugrid=z[f"pair{k}_ugrid"]))
+    return tabs
+
+
+def load_tables(name):
+    """Pair tables pi-qmc built for a configuration (tables_<name>.npz)."""
+    z = np.load(os.path.join(GOLDEN, "tables_" + name + ".npz"))
+    return dict(kw=ast.literal_eval(str(z["config"])), tables=_pair_tables(z))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    kw = ast.literal_eval(str(z["config"]))
+    tabs = _pair_tables(z)
     ew = None
     if "ewald_kvec" in z:
         ew = dict(totk=len(z["ewald_vk"]), kvec=z["ewald_kvec"], vk=z["ewald_vk"],

@@ -1,50 +1,77 @@
-"""Energies of the mixed-precision form against the FP64 form.
+"""Thermodynamic energies of equilibrated chains against the reference.
 
-The mixed form (FP32 pair-action and nodal-action terms summed in FP64, FP32
-Box-Muller proposals, FP64 determinants) must give the same thermodynamic
-energy as the FP64 form within two standard errors.  Both run the same replicas
-from the same paths and counter streams (the proposals differ in their FP32
-transform, so the chains separate); each standard error comes from the spread
-over independent replicas after equilibration.  Tolerance:
-|E_mixed - E_fp64| <= 2 sqrt(sigma_mixed^2 + sigma_fp64^2).
+* pi-qmc's SHO system test (test/system/sho/test_sho.py:25-32): one electron
+  with SHOAction omega = 0.5, kT = 1, M = 32, level 5.  The harmonic link action
+  is exact, so the estimator's mean is 3/2 omega coth(omega / 2kT) =
+  0.75 coth(0.25) at any M; pi-qmc accepts +-0.08 around it.
+* pi-qmc's own equilibrated energies (tests/golden/energy_<case>.npz, made by
+  tests/golden/make_energy.py with oracle/_ref) for the plain Coulomb dot of
+  config 1 (N=2, beta=10, M=256, L=4) and a small fixed-node dot (N=4,
+  SHONodes), each in the FP64 form and in the mixed form.  The criterion is
+  |E_engine - E_pi-qmc| <= 2 sqrt(sigma_engine^2 + sigma_pi-qmc^2).
+
+Engine standard errors come from the spread of per-replica means over 512
+(1024 for the SHO test) independent replicas, each its own Markov chain,
+measured once per sweep after the same equilibration as the reference's.
 """
 import math
 
 import numpy as np
 import pytest
 
+import golden_io
 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
 
-def run(pimc, kw, tabs, paths, precision, nrep, steps, attempts):
-    e = pimc.Engine(kw, nrep, tabs, None, seed=4242, precision=precision)
-    e.upload_paths(paths)
-    e.run_steps(attempts, steps // 2, energies=False)  # equilibration
-    E = e.run_steps(attempts, steps - steps // 2)    # [steps][replicas]
-    e.close()
-    per_rep = E.mean(axis=0)
-    return per_rep.mean(), per_rep.std(ddof=1) / math.sqrt(nrep), per_rep
+@pytest.fixture(scope="module")
+def pimc():
+    import pimc_gb300
+    pimc_gb300.build.build()
+    return pimc_gb300
 
 
-@pytest.mark.parametrize("name,kw", [
-    ("dot4_fn", W.dot20_fn(counts=[2, 2], nslice=64, beta=4.0, nlevel=3)),
-    ("dot2", W.dot2(nslice=128)),
-])
-def test_mixed_energy_within_two_sigma(name, kw):
-    import pimc_gb300 as pimc
-    tabs, _ = pimc.coulomb_tables(kw)
-    nrep = 512
-    kind = "const" if any(kw.get("node_kind", [0])) else "gauss"
+def sweep_attempts(kw):
+    return -(-kw["nslice"] // (1 << kw["nlevel"])) * sum(kw["counts"])
 
+
+def equilibrated_energy(pimc, kw, tables, kind, precision, nrep, equil, measure, attempts):
     class _C:
         nslice, npart, cell = kw["nslice"], sum(kw["counts"]), [kw["cell"]] * 3
 
-    paths = [W.initial_path(_C, kind, seed=900 + r) for r in range(nrep)]
-    sweep = sum(kw["counts"]) * kw["nslice"] // (1 << kw["nlevel"])
-    e64, s64, r64 = run(pimc, kw, tabs, paths, pimc.PIMC_PREC_FP64, nrep, 40, sweep)
-    emx, smx, rmx = run(pimc, kw, tabs, paths, pimc.PIMC_PREC_MIXED, nrep, 40, sweep)
-    assert np.all(np.isfinite(r64)) and np.all(np.isfinite(rmx))
-    assert s64 > 0
-    assert abs(emx - e64) <= 2 * math.hypot(s64, smx), (name, emx, e64, s64, smx)
+    e = pimc.Engine(kw, nrep, tables, None, seed=808, precision=precision)
+    e.upload_paths([W.initial_path(_C, kind, seed=3000 + r) for r in range(nrep)])
+    e.run_steps(attempts, equil, energies=False)
+    E = e.run_steps(attempts, measure)  # [measure][nrep]
+    acc, att, st = e.replica_status()
+    e.close()
+    assert np.all(st == 0) and np.all(np.isfinite(E))
+    per_rep = E.mean(axis=0)
+    return float(per_rep.mean()), float(per_rep.std(ddof=1) / math.sqrt(nrep))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sho_system_energy(pimc, precision):
+    # pi-qmc's input: 100 thermalising attempts, then a measurement after every
+    # attempt (one attempt is one sweep of this one-particle ring).
+    g = golden_io.load("sho_system")
+    e, sig = equilibrated_energy(pimc, g["kw"], [], "gauss", precision, 1024, 100, 500, 1)
+    exact = 0.75 / math.tanh(0.25)
+    assert abs(e - exact) <= 0.08, (e, sig)
+    assert abs(e - exact) <= 3 * sig, (e, sig, exact)
+    assert sig < 0.041  # pi-qmc's own run reaches an error bar of 0.041
+
+
+@pytest.mark.parametrize("case,kind,equil,measure",
+                         [("dot2_full", "gauss", 500, 600), ("dot4_fn", "const", 300, 400)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_energy_matches_pi_qmc(pimc, case, kind, equil, measure, precision):
+    ref = np.load(golden_io.GOLDEN + "/energy_" + case + ".npz")
+    g = golden_io.load(case)
+    e, sig = equilibrated_energy(pimc, g["kw"], g["tables"], kind, precision, 512, equil,
+                                 measure, sweep_attempts(g["kw"]))
+    er, sr = float(ref["energy"]), float(ref["sigma"])
+    assert ref["block_means"].size >= 50
+    assert abs(e - er) <= 2 * math.hypot(sig, sr), (case, precision, e, sig, er, sr)
+    assert sig <= 0.01 * abs(er)

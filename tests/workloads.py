@@ -23,6 +23,10 @@ GOLDEN_CASES = {
     # action, no harmonic action, on three electrons of two species
     "dot3_prim": (dot2(counts=[2, 1], sho_omega=[0.0, 0.0], prim_a=[0.5, 0.3],
                        prim_b=[0.05, 0.1], nslice=64, nlevel=3, beta=4.0), "gauss", 500),
+    # pi-qmc's SHO system test (test/system/sho/pimc.xml): one electron,
+    # SHOAction omega = 0.5, kT = 1, M = 32, level 5 (a section spans the ring)
+    "sho_system": (dot2(counts=[1], sho_omega=[0.5], nslice=32, beta=1.0, nlevel=5, coulomb=0,
+                        cell=20.0), "gauss", 600),
 }
 
 # NodeModel fixtures (tests/golden/nodes_<case>.npz): pi-qmc's own
