@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="timed seconds of the engine line's all-core CPU baseline")
     p.add_argument("--equil", type=int, default=-1,
-                   help="untimed equilibration steps before the warm-up (-1: per workload)")
+                   help="untimed equilibration rounds before the warm-up (-1: per workload)")
     p.add_argument("--serve-requests", type=int, default=600,
                    help="requests of the serving sub-run in the default line (0: none)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -515,9 +515,14 @@ def run_engine(args, rank, world):
     reach = [depth_reach[L - lev] for lev in range(L + 1)]
     eng.upload_paths(paths)
     # equilibration (untimed): the energy block below is taken on equilibrated chains
-    equil = args.equil if args.equil >= 0 else default_equil(args.workload)
-    if equil:
-        eng.run_steps(A, equil, energies=False)
+    rounds, ndisp, nsweep = default_equil(args.workload)
+    if args.equil >= 0:
+        rounds = args.equil
+    for _ in range(rounds):
+        if ndisp:
+            eng.run_displace(ndisp, [1.0, 1.0, 1.0], 1, -1)
+        eng.run_steps(A, nsweep, energies=False)
+    equil = rounds * nsweep
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         eng.run_steps(A, 1, energies=False)
@@ -543,7 +548,9 @@ def run_engine(args, rank, world):
     units = A * sum((1 << k["nlevel"]) - 1 for k in systems)
     value = world * units * args.steps / (t_ms * 1e-3)
     energy_block = energy_stats(E, f"the {args.steps} timed steps, after {equil} equilibration "
-                                   f"and {args.warmup} warm-up steps from the initial paths")
+                                   f"sweeps ({rounds * ndisp} rigid displacement attempts of one "
+                                   f"particle's path, uniform in a 1 bohr box, among them) and "
+                                   f"{args.warmup} warm-up steps from the initial paths")
     energy_block.update(energy_vs_reference(args.workload, energy_block, equil + args.warmup))
     # ---- end to end through the public API: each step uploads the chain's
     # current paths from pinned host memory, runs the sweep, measures, and
@@ -562,6 +569,10 @@ def run_engine(args, rank, world):
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = world * units * e2e_steps / e2e_s
     assert np.all(np.isfinite(e2e_energy))
+    # ---- the mixed form's error per result against the FP64 form (untimed)
+    if args.precision == "mixed" and not batch:
+        energy_block["precision_error"] = precision_report(pimc_gb300, kw, tabs, ew, paths, R, A,
+                                                           seed, stream)
     # ---- the plain form: one replica, FP64, same sweep (untimed by the step loop)
     plain = None if batch else pimc_gb300.Engine(kw, 1, tabs, ew, seed=seed)
     plain_value = None
@@ -618,15 +629,73 @@ def run_engine(args, rank, world):
     return out
 
 
+def precision_report(pimc_gb300, kw, tabs, ew, paths, R, A, seed, stream):
+    """Error of every mixed-form result against the FP64 form on identical
+    inputs.  Both forms draw the same FP64 proposals, so a mixed chain and an
+    FP64 chain started from the same path and stream make the same moves until
+    a decision differs (a uniform within the mixed error of its acceptance
+    probability); on those common attempts each level's action difference,
+    fixed-node difference and ln T are compared.  The thermodynamic estimator
+    is compared on identical paths (the FP64 chain's final paths measured by
+    both engines)."""
+    nr = min(R, 152)
+    n_att = min(A, 128)
+    per = 3 * kw["nslice"] * sum(kw["counts"])
+    sub = paths[:nr * per]
+    L = kw["nlevel"]
+    recs, engs = [], []
+    for prec in (pimc_gb300.PIMC_PREC_MIXED, pimc_gb300.PIMC_PREC_FP64):
+        e = pimc_gb300.Engine(kw, nr, tabs, ew, seed=seed, precision=prec)
+        e.set_stream(stream.cuda_stream)
+        e.upload_paths(sub)
+        recs.append(e.run_sections(n_att, records=True))
+        engs.append(e)
+    m, f = recs
+    same = np.ones(nr, bool)
+    common = np.zeros((nr, n_att), bool)
+    for a in range(n_att):
+        ok = ((m["reject_level"][:, a] == f["reject_level"][:, a]) &
+              (m["ipart"][:, a] == f["ipart"][:, a]) & (m["ifirst1"][:, a] == f["ifirst1"][:, a]))
+        common[:, a] = same
+        same &= ok
+    out = {"replicas": nr, "attempts": n_att, "compared_attempts": int(common.sum()),
+           "chains_identical_throughout": int(same.sum()), "per_level": []}
+    for lev in range(L + 1):
+        row = {"level": lev}
+        for key in ("ds", "ds_node", "lnt"):
+            a, b = m[key][:, :, lev], f[key][:, :, lev]
+            # a level's values exist where the FP64 chain evaluated it
+            ev = common & ((f["reject_level"] < 0) | (f["reject_level"] <= lev))
+            d = np.abs(a - b)[ev & (np.abs(b) < 1e99)]
+            row[key] = {"max": float(d.max()) if d.size else None,
+                        "rms": float(np.sqrt(np.mean(d * d))) if d.size else None,
+                        "n": int(d.size)}
+        out["per_level"].append(row)
+    fin = engs[1].download_paths(flat=True)
+    engs[0].upload_paths(fin)
+    e_m, e_f = engs[0].thermo_energy(), engs[1].thermo_energy()
+    de = np.abs(e_m - e_f)
+    out["thermo_energy"] = {"max": float(de.max()), "rms": float(np.sqrt(np.mean(de * de))),
+                            "relative_max": float((de / np.abs(e_f)).max())}
+    for e in engs:
+        e.close()
+    return out
+
+
 def default_equil(name):
-    # untimed sweeps before the warm-up: the chains of the dots start from
-    # constant-in-time (or per-slice Gaussian) paths
-    return {"dot20_fn": 100, "dot2": 200, "heg54": 0, "batch4096": 0, "serve": 0}[name]
+    """Untimed equilibration before the warm-up: (rounds, rigid-displacement
+    attempts per replica per round, sweeps per round).  Bisection moves shift a
+    path's centroid only slowly; from constant-in-time paths the config-2 dot's
+    chains still spread ~175 Ha apart after 150 sweeps of bisection alone, while
+    pi-qmc's DisplaceMoveSampler moves (whole-path shifts) bring them to a
+    ~30 Ha spread and the mean from ~195 to ~146 Ha within 50 sweeps."""
+    return {"dot20_fn": (10, 20, 5), "dot2": (40, 0, 5), "heg54": (0, 0, 1),
+            "batch4096": (0, 0, 1), "serve": (0, 0, 1)}[name]
 
 
 # equilibrated energies of pi-qmc's own code (tests/golden/make_energy.py) for
 # the bench workloads that have one
-REFERENCE_ENERGY = {"dot20_fn": "dot20_fn", "dot2": "dot2_full"}
+REFERENCE_ENERGY = {"dot2": "dot2_full"}
 
 
 def energy_vs_reference(name, block, equil_steps):

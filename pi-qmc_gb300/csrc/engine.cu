@@ -294,6 +294,12 @@ void fill_sys(const pimc_system& s, DevSys& d) {
         const double wt = s.sho_omega[i] * s.tau * nStride;
         d.sho_cosh[lev][i] = std::cosh(wt);
         d.sho_div1[lev][i] = 1.0 / (2.0 * std::sinh(wt));
+        // x coth x - 1 by its series below 0.1 (x^2/3 - x^4/45 + 2x^6/945 - x^8/4725)
+        const double x2 = wt * wt;
+        const double xc = wt < 0.1 ? x2 * (1.0 / 3 - x2 * (1.0 / 45 - x2 * (2.0 / 945 - x2 / 4725)))
+                                   : wt / std::tanh(wt) - 1.0;
+        d.sho_a[lev][i] = (float)(s.spec_mass[i] * 0.5 / (s.tau * nStride) * xc);
+        d.sho_b[lev][i] = (float)(s.spec_mass[i] * s.sho_omega[i] * std::tanh(0.5 * wt));
       }
     }
   }

@@ -181,24 +181,17 @@ static __device__ __noinline__ void store_section(const DevSys& s, double* path,
 // moving particle at one level; threads own moved slices.  Returns ln(T_old/T_new).
 // Every normal the attempt's mover can use, drawn in parallel before the
 // levels: moved slice `ord` (0 .. 2^L - 2 in FreeMover's order) takes Box-Muller
-// pairs 2 ord and 2 ord + 1 and uses the first three values (FP32 transform
-// in the mixed form).
+// pairs 2 ord and 2 ord + 1 and uses the first three values.  Both precision
+// forms draw the same FP64 normals, so a mixed-form chain makes the FP64
+// chain's proposals and its action differences can be compared with the FP64
+// form's on identical moves.
 static __device__ __noinline__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t seed,
                                        uint32_t rep, uint32_t att) {
   const int nord = (1 << s.nlevel) - 1;
   for (int o = threadIdx.x; o < nord; o += blockDim.x) {
     double z0, z1, z2, z3;
-    if (s.mixed) {
-      float f0, f1, f2, f3;
-      stream_normal_pair_f(seed, rep, att, 2u * o, &f0, &f1);
-      stream_normal_pair_f(seed, rep, att, 2u * o + 1u, &f2, &f3);
-      z0 = f0;
-      z1 = f1;
-      z2 = f2;
-    } else {
-      stream_normal_pair(seed, rep, att, 2u * o, &z0, &z1);
-      stream_normal_pair(seed, rep, att, 2u * o + 1u, &z2, &z3);
-    }
+    stream_normal_pair(seed, rep, att, 2u * o, &z0, &z1);
+    stream_normal_pair(seed, rep, att, 2u * o + 1u, &z2, &z3);
     m.nrm[3 * o] = z0;
     m.nrm[3 * o + 1] = z1;
     m.nrm[3 * o + 2] = z2;
@@ -600,6 +593,7 @@ static __device__ __noinline__ double node_level(const DevSys& s, const Smem& m,
   if (m.ictl[C_FLAG]) return 2e100;
   if (level != 0) return 0.0;
   double part = 0.0;
+  FSum fpart;
   for (int it = threadIdx.x; it < (nsec - 1) * n; it += blockDim.x) {
     const int t = 1 + it / n, p = it % n;
     const double* D0 = m.dist + (t * 2) * nsm;
@@ -608,19 +602,20 @@ static __device__ __noinline__ double node_level(const DevSys& s, const Smem& m,
     const double* Np0 = m.ndist + ((t - 1) * 2) * nsm;
     if (s.mixed) {
       // FP32 terms (1 - e^-x through expm1 keeps them accurate near the node),
-      // summed in FP64
+      // their sum compensated
       const float a1 = -expm1f(-(float)(D0[p] * Dp0[p]));
       const float b1 = -expm1f(-(float)(N0[p] * Np0[p]));
       const float a2 = -expm1f(-(float)(D0[nsm + p] * Dp0[nsm + p]));
       const float b2 = -expm1f(-(float)(N0[nsm + p] * Np0[nsm + p]));
-      part += (double)(logf(a1) - logf(b1)) + (double)(logf(a2) - logf(b2));
+      fpart.add(logf(a1) - logf(b1));
+      fpart.add(logf(a2) - logf(b2));
       continue;
     }
     double a = log((1 - exp(-D0[p] * Dp0[p])) / (1 - exp(-N0[p] * Np0[p])));
     a += log((1 - exp(-D0[nsm + p] * Dp0[nsm + p])) / (1 - exp(-N0[nsm + p] * Np0[nsm + p])));
     part += a;
   }
-  return block_sum(part, m.red);
+  return block_sum(s.mixed ? fpart.value() : part, m.red);
 }
 
 // The uniform-stream index of the first uniform consumed at `level`

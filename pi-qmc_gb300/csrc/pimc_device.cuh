@@ -44,6 +44,9 @@ struct DevSys {
   double sho_cosh[kMaxLevels][kMaxSpecies], sho_div1[kMaxLevels][kMaxSpecies];
   double sho_div2[kMaxLevels];
   double sho_coth[kMaxSpecies], sho_csch[kMaxSpecies], sho_cosh0[kMaxSpecies];
+  // The mixed form's SHO link action without cancellation:
+  // a |r1 - r0|^2 + b r0.r1, a = (m / 2 tau') (x coth x - 1), b = m w tanh(x / 2), x = w tau'
+  float sho_a[kMaxLevels][kMaxSpecies], sho_b[kMaxLevels][kMaxSpecies];
   double cell[3], cellb[3], rcut2;
   int spring, coulomb, ewald, mover, fixed_node;
   int mixed;  // PIMC_PREC_MIXED: pair-action terms in FP32, accumulated in FP64
@@ -133,17 +136,21 @@ __device__ __forceinline__ double pg_eval(double nome, double pref, double k, in
 
 // Pair-action table lookup on the logarithmic grid
 // (PairAction::u00 / uk0 / uk0CalcDerivatives, src/action/PairAction.cc:601-655).
+// The range tests come before the conversion to an integer and are written so
+// that a NaN or infinite distance takes a clamped branch: converting NaN to int
+// is not defined to give an in-range index.  For finite q >= 1 the branches
+// are pi-qmc's (i = int(x) > ngpts - 2 exactly when x >= ngpts - 1).
 __device__ __forceinline__ void tab_locate(const DevTable& t, double q, int& i, double& x) {
   q *= t.rgridinv;
   x = log(q) * t.logrratioinv;
-  i = (int)x;
-  if (q < 1) {
+  if (!(q >= 1)) {
     i = 0;
     x = 0;
-  } else if (i > t.ngpts - 2) {
+  } else if (!(x < t.ngpts - 1)) {
     i = t.ngpts - 2;
     x = 1;
   } else {
+    i = (int)x;
     x -= i;
   }
 }
@@ -186,14 +193,15 @@ __device__ __forceinline__ void tab_uk0d(const DevTable& t, double q, double s2,
 __device__ __forceinline__ float tab_uk0_f(const DevTable& t, float q, float s2, int norder_eff) {
   q *= (float)t.rgridinv;
   float x = __logf(q) * (float)t.logrratioinv;
-  int i = (int)x;
-  if (q < 1.f) {
+  int i;  // range tests before the conversion, as tab_locate
+  if (!(q >= 1.f)) {
     i = 0;
     x = 0.f;
-  } else if (i > t.ngpts - 2) {
+  } else if (!(x < (float)(t.ngpts - 1))) {
     i = t.ngpts - 2;
     x = 1.f;
   } else {
+    i = (int)x;
     x -= i;
   }
   const float* g0 = t.ugrid32 + (size_t)i * 2 * t.ndata;
@@ -207,14 +215,15 @@ __device__ __forceinline__ float tab_uk0_f(const DevTable& t, float q, float s2,
 __device__ __forceinline__ float tab_uk0d_tau_f(const DevTable& t, float q, float s2) {
   q *= (float)t.rgridinv;
   float x = __logf(q) * (float)t.logrratioinv;
-  int i = (int)x;
-  if (q < 1.f) {
+  int i;  // range tests before the conversion, as tab_locate
+  if (!(q >= 1.f)) {
     i = 0;
     x = 0.f;
-  } else if (i > t.ngpts - 2) {
+  } else if (!(x < (float)(t.ngpts - 1))) {
     i = t.ngpts - 2;
     x = 1.f;
   } else {
+    i = (int)x;
     x -= i;
   }
   const float* g0 = t.ugrid32 + (size_t)i * 2 * t.ndata + t.ndata;
@@ -230,6 +239,19 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
   const double bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
+
+// A compensated FP32 sum (Knuth's TwoSum per term, the rounding errors
+// collected in a second float): the mixed form's sums over links and pairs.
+struct FSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float t) {
+    const float u = __fadd_rn(s, t);
+    const float bb = __fsub_rn(u, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb)));
+    s = u;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
 
 // Deterministic block sum of one double per thread (fixed tree order).
 __device__ __forceinline__ double block_sum(double v, double* red) {

@@ -200,24 +200,6 @@ PIMC_HD void stream_normal_pair(uint64_t seed, uint32_t replica, uint32_t attemp
   *z1 = PR_MUL(rad, s);
 }
 
-#ifdef __CUDACC__
-// FP32 Box-Muller pair from the same Philox block as stream_normal_pair (the
-// mixed-precision form's proposals): 24-bit uniforms in (0,1), so |z| < 5.8.
-__device__ __forceinline__ void stream_normal_pair_f(uint64_t seed, uint32_t replica,
-                                                     uint32_t attempt, uint32_t pair, float* z0,
-                                                     float* z1) {
-  const Philox4 b = philox4x32_10(pair, attempt, replica, kStreamNormal,
-                                  (uint32_t)seed, (uint32_t)(seed >> 32));
-  const float u1 = ((float)(b.v[0] >> 8) + 0.5f) * 5.9604644775390625e-8f;  // 2^-24
-  const float u2 = ((float)(b.v[2] >> 8) + 0.5f) * 5.9604644775390625e-8f;
-  const float rad = sqrtf(-2.0f * logf(u1));
-  float sn, cs;
-  sincospif(2.0f * u2, &sn, &cs);
-  *z0 = rad * cs;
-  *z1 = rad * sn;
-}
-#endif
-
 PIMC_HD double stream_normal(uint64_t seed, uint32_t replica, uint32_t attempt,
                              uint32_t k) {
   double z0, z1;

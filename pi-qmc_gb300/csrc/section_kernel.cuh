@@ -462,8 +462,13 @@ static __device__ void node_eval_warp(const DevSys& s, int sp, const SliceView& 
 // (src/action/PrimSHOAction.cc:21-58), PairAction per species pair
 // (src/action/PairAction.cc:219-360).  Work items are links and (partner, link)
 // pairs; each item contributes (new - old).
+static __device__ __noinline__ double action_partial_mixed(const DevSys& s, const Smem& m,
+                                                          int ipart, int level, int tid,
+                                                          int nthreads);
+
 static __device__ __noinline__ double action_partial(const DevSys& s, const Smem& m, int ipart, int level,
                                         int tid, int nthreads) {
+  if (s.mixed) return action_partial_mixed(s, m, ipart, level, tid, nthreads);
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
   const int nlinks = 1 << (L - level);
@@ -561,35 +566,6 @@ static __device__ __noinline__ double action_partial(const DevSys& s, const Smem
     const double pjx1 = m.s1x[t1 * np + j], pjy1 = m.s1y[t1 * np + j], pjz1 = m.s1z[t1 * np + j];
     const double pjx0 = m.s1x[t0 * np + j], pjy0 = m.s1y[t0 * np + j], pjz0 = m.s1z[t0 * np + j];
     const bool offdiag = level < 3 && t.norder > 0;
-    if (s.mixed) {
-      // FP32 pair terms (the O(N) part), their difference accumulated in FP64.
-      float actf[2];
-#pragma unroll
-      for (int pass = 0; pass < 2; ++pass) {
-        double ax, ay, az, bx, by, bz;
-        if (pass == 0) {
-          ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
-          bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
-        } else {
-          ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
-          bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
-        }
-        double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
-        pbc(s, dx, dy, dz);
-        double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
-        pbc(s, px, py, pz);
-        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-        const float gx = (float)px, gy = (float)py, gz = (float)pz;
-        const float r = sqrtf(fx * fx + fy * fy + fz * fz);
-        const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
-        const float qq = 0.5f * (r + rp);
-        const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
-        const float s2 = offdiag ? __fdividef(sx * sx + sy * sy + sz * sz, qq * qq) : 0.f;
-        actf[pass] = tab_uk0_f(t, qq, s2, offdiag ? t.norder : 0) * (float)nStride;
-      }
-      acc += (double)(actf[0] - actf[1]);
-      continue;
-    }
     double act[2];
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
@@ -621,6 +597,132 @@ static __device__ __noinline__ double action_partial(const DevSys& s, const Smem
     acc += act[0] - act[1];
   }
   return acc;
+}
+
+// The mixed form of action_partial: every term in FP32, the per-thread sum
+// compensated (FSum) and returned in FP64 for the block reduction.  Spring:
+// (|d_new|^2 - |d_old|^2) / (4 lambda tau'); SHO: a (|d_new|^2 - |d_old|^2) +
+// b (r0.r1_new - r0.r1_old), the harmonic link action minus its free part
+// rearranged so that nothing cancels (sho_a, sho_b); PrimSHO: (a x^2 + b x^4)
+// tau' at the moved bead; pairs: PairAction's u00 / uk0 series on the FP32 copy
+// of the table.  Differences of positions are formed (and minimum-imaged) in
+// FP64 before they are rounded to FP32.
+static __device__ __noinline__ double action_partial_mixed(const DevSys& s, const Smem& m,
+                                                          int ipart, int level, int tid,
+                                                          int nthreads) {
+  const int L = s.nlevel, np = s.npart;
+  const int nStride = 1 << level;
+  const int nlinks = 1 << (L - level);
+  int sp = 0;
+  for (int k = 0; k < s.nspecies; ++k)
+    if (ipart >= s.spec_first[k] && ipart < s.spec_first[k] + s.spec_count[k]) sp = k;
+  FSum acc;
+  const float inv2s2 = (float)s.spr_inv2s2[level][sp];
+  const bool sho = s.sho_omega[sp] > 0;
+  const float sa = s.sho_a[level][sp], sb = s.sho_b[level][sp];
+  const bool prim = s.prim_a[sp] != 0 || s.prim_b[sp] != 0;
+  const float pa = (float)s.prim_a[sp], pb = (float)s.prim_b[sp];
+  const float ktau = (float)(s.tau * nStride);
+  int tb[kMaxTables], tjb[kMaxTables], tn[kMaxTables], nt = 0;
+  if (s.coulomb) {
+    for (int ti = 0; ti < s.ntab; ++ti) {
+      const DevTable& t = s.tab[ti];
+      if (ipart >= t.ifirst1 && ipart < t.ifirst1 + t.npart1) {
+        tb[nt] = ti;
+        tjb[nt] = t.ifirst2;
+        tn[nt++] = t.npart2;
+      } else if (ipart >= t.ifirst2 && ipart < t.ifirst2 + t.npart2) {
+        tb[nt] = ti;
+        tjb[nt] = t.ifirst1;
+        tn[nt++] = t.npart1;
+      }
+    }
+  }
+  int total = nlinks;
+  for (int q = 0; q < nt; ++q) total += tn[q] * nlinks;
+  for (int item = tid; item < total; item += nthreads) {
+    if (item < nlinks) {
+      const int k = item + 1;
+      const int t1 = k * nStride, t0 = t1 - nStride;
+      const double n1x = m.mx[t1], n1y = m.my[t1], n1z = m.mz[t1];
+      const double n0x = m.mx[t0], n0y = m.my[t0], n0z = m.mz[t0];
+      const double o1x = m.s1x[t1 * np + ipart], o1y = m.s1y[t1 * np + ipart], o1z = m.s1z[t1 * np + ipart];
+      const double o0x = m.s1x[t0 * np + ipart], o0y = m.s1y[t0 * np + ipart], o0z = m.s1z[t0 * np + ipart];
+      if (s.spring) {
+        double dx = n1x - n0x, dy = n1y - n0y, dz = n1z - n0z;
+        pbc(s, dx, dy, dz);
+        double ex = o1x - o0x, ey = o1y - o0y, ez = o1z - o0z;
+        pbc(s, ex, ey, ez);
+        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+        const float gx = (float)ex, gy = (float)ey, gz = (float)ez;
+        acc.add(inv2s2 * ((fx * fx + fy * fy + fz * fz) - (gx * gx + gy * gy + gz * gz)));
+      }
+      if (sho) {
+        const float a0x = (float)n0x, a0y = (float)n0y, a0z = (float)n0z;
+        const float a1x = (float)n1x, a1y = (float)n1y, a1z = (float)n1z;
+        const float b0x = (float)o0x, b0y = (float)o0y, b0z = (float)o0z;
+        const float b1x = (float)o1x, b1y = (float)o1y, b1z = (float)o1z;
+        const float dnx = (float)(n1x - n0x), dny = (float)(n1y - n0y), dnz = (float)(n1z - n0z);
+        const float dox = (float)(o1x - o0x), doy = (float)(o1y - o0y), doz = (float)(o1z - o0z);
+        const float dd = (dnx * dnx + dny * dny + dnz * dnz) - (dox * dox + doy * doy + doz * doz);
+        const float rr = (a0x * a1x + a0y * a1y + a0z * a1z) - (b0x * b1x + b0y * b1y + b0z * b1z);
+        acc.add(sa * dd + sb * rr);
+      }
+      if (prim && k < nlinks) {
+        double x = n1x, y = n1y, z = n1z;
+        pbc(s, x, y, z);
+        const float xn = (float)x, yn = (float)y, zn = (float)z;
+        x = o1x;
+        y = o1y;
+        z = o1z;
+        pbc(s, x, y, z);
+        const float xo = (float)x, yo = (float)y, zo = (float)z;
+        const float r2n = xn * xn + yn * yn + zn * zn, r2o = xo * xo + yo * yo + zo * zo;
+        acc.add((pa * (r2n - r2o) + pb * (r2n * r2n - r2o * r2o)) * ktau);
+      }
+      continue;
+    }
+    int it = item - nlinks, q = 0;
+    while (it >= tn[q] * nlinks) {
+      it -= tn[q] * nlinks;
+      ++q;
+    }
+    const DevTable& t = s.tab[tb[q]];
+    const int jj = it / nlinks;
+    const int j = tjb[q] + jj;
+    if (j == ipart) continue;
+    const int k = it - jj * nlinks + 1;
+    const int t1 = k * nStride, t0 = t1 - nStride;
+    const double pjx1 = m.s1x[t1 * np + j], pjy1 = m.s1y[t1 * np + j], pjz1 = m.s1z[t1 * np + j];
+    const double pjx0 = m.s1x[t0 * np + j], pjy0 = m.s1y[t0 * np + j], pjz0 = m.s1z[t0 * np + j];
+    const bool offdiag = level < 3 && t.norder > 0;
+    float actf[2];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      double ax, ay, az, bx, by, bz;
+      if (pass == 0) {
+        ax = m.mx[t1]; ay = m.my[t1]; az = m.mz[t1];
+        bx = m.mx[t0]; by = m.my[t0]; bz = m.mz[t0];
+      } else {
+        ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
+        bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
+      }
+      double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
+      pbc(s, dx, dy, dz);
+      double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
+      pbc(s, px, py, pz);
+      const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+      const float gx = (float)px, gy = (float)py, gz = (float)pz;
+      const float r = sqrtf(fx * fx + fy * fy + fz * fz);
+      const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
+      const float qq = 0.5f * (r + rp);
+      const float sx = fx - gx, sy = fy - gy, sz = fz - gz;
+      const float s2 = offdiag ? __fdividef(sx * sx + sy * sy + sz * sz, qq * qq) : 0.f;
+      actf[pass] = tab_uk0_f(t, qq, s2, offdiag ? t.norder : 0) * (float)nStride;
+    }
+    acc.add(actf[0] - actf[1]);
+  }
+  return acc.value();
 }
 
 // e^{ik.r} factor tables of one bead, column `col` of X [nx][w], Y [ny][w] and

@@ -29,9 +29,6 @@ PROCS = 8
 CASES = {
     "dot2_full": ("dot2_full", "gauss", 2000, 16, 1500),
     "dot4_fn": ("dot4_fn", "const", 1000, 16, 500),
-    # the fixed-node dot of config 2 (N=20, SHONodes, beta=20, M=1024, L=5),
-    # from constant-in-time paths
-    "dot20_fn": ("dot20_fn", "const", 100, 16, 25),
 }
 SEED = 5150
 

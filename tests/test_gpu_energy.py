@@ -3,7 +3,13 @@
 * pi-qmc's SHO system test (test/system/sho/test_sho.py:25-32): one electron
   with SHOAction omega = 0.5, kT = 1, M = 32, level 5.  The harmonic link action
   is exact, so the estimator's mean is 3/2 omega coth(omega / 2kT) =
-  0.75 coth(0.25) at any M; pi-qmc accepts +-0.08 around it.
+  0.75 coth(0.25) at any M; pi-qmc accepts +-0.08 around it.  The cell is 200
+  bohr, not the input's 20: FreeMover takes every new bead to its minimum image,
+  so in a 20-bohr cell a bead that strays past 10 bohr lands on the far side of
+  the box and the estimator's SHO term, which uses the raw positions, spikes
+  (with pi-qmc's own algorithm one chain of these 1024 then averages -667 and
+  the mean comes out 2.40 +- 0.66, the engine's value to every digit); the
+  analytic value is that of the unbounded oscillator.
 * pi-qmc's own equilibrated energies (tests/golden/energy_<case>.npz, made by
   tests/golden/make_energy.py with oracle/_ref) for the plain Coulomb dot of
   config 1 (N=2, beta=10, M=256, L=4) and a small fixed-node dot (N=4,
@@ -56,7 +62,8 @@ def test_sho_system_energy(pimc, precision):
     # pi-qmc's input: 100 thermalising attempts, then a measurement after every
     # attempt (one attempt is one sweep of this one-particle ring).
     g = golden_io.load("sho_system")
-    e, sig = equilibrated_energy(pimc, g["kw"], [], "gauss", precision, 1024, 100, 500, 1)
+    kw = dict(g["kw"], cell=200.0)
+    e, sig = equilibrated_energy(pimc, kw, [], "gauss", precision, 1024, 100, 500, 1)
     exact = 0.75 / math.tanh(0.25)
     assert abs(e - exact) <= 0.08, (e, sig)
     assert abs(e - exact) <= 3 * sig, (e, sig, exact)

@@ -465,3 +465,43 @@ def test_displace_matches_golden(pimc, case):
     assert rel_close(r["ds"][0], ref["ds"], 1e-11)
     assert rel_close(r["ds_node"][0], ref["ds_node"], 1e-9)
     assert np.abs(e.download_paths()[0] - d["path"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("case", ["dot4_fn", "dot2_full", "heg8"])
+def test_mixed_form_on_identical_proposals(pimc, case):
+    # Both precision forms draw the same FP64 proposals, so a mixed chain follows
+    # the FP64 chain until a uniform falls within the mixed error of its
+    # acceptance probability.  On the common attempts: ln T bit for bit (the
+    # mover is FP64 in both), action differences (FP32 terms, compensated sums)
+    # within 1e-4 of max(|dS|, 1), fixed-node differences within 1e-4 of
+    # max(|dS_node|, 1); the thermodynamic estimator on identical paths within
+    # 1e-5 relative.
+    g = golden_io.load(case)
+    n, R = 150, 8
+    out = []
+    for prec in (1, 0):
+        e = pimc.Engine(g["kw"], R, g["tables"], g["ewald"], seed=515, precision=prec)
+        e.upload_paths([g["path0"]] * R)
+        out.append((e, e.run_sections(n, records=True)))
+    (em, m), (ef, f) = out
+    same = np.ones(R, bool)
+    compared = 0
+    nl = g["kw"]["nlevel"] + 1
+    for a in range(n):
+        ok = ((m["reject_level"][:, a] == f["reject_level"][:, a]) &
+              (m["ipart"][:, a] == f["ipart"][:, a]))
+        for r in np.nonzero(same & ok)[0]:
+            compared += 1
+            lv = slice(0, nl)
+            assert np.array_equal(m["lnt"][r, a, lv], f["lnt"][r, a, lv])
+            fin = np.abs(f["ds"][r, a, lv]) < 1e99
+            assert np.all(np.abs(m["ds"][r, a, lv] - f["ds"][r, a, lv])[fin]
+                          <= 1e-4 * np.maximum(np.abs(f["ds"][r, a, lv][fin]), 1.0))
+            fn = np.abs(f["ds_node"][r, a, lv]) < 1e99
+            assert np.array_equal(np.abs(m["ds_node"][r, a, lv]) >= 1e99, ~fn)
+            assert np.all(np.abs(m["ds_node"][r, a, lv] - f["ds_node"][r, a, lv])[fn]
+                          <= 1e-4 * np.maximum(np.abs(f["ds_node"][r, a, lv][fn]), 1.0))
+        same &= ok
+    assert compared >= n * R // 2
+    em.upload_paths(ef.download_paths())
+    assert np.allclose(em.thermo_energy(), ef.thermo_energy(), rtol=1e-5, atol=0)

@@ -82,20 +82,3 @@ def test_crossed_node_initial_path(pimc):
     assert broken["upload_status"][1] == 0
     assert broken["status"][1] & pimc.PIMC_STATUS_INIT_CROSSING
     assert_others_unaffected(clean, broken)
-
-
-def test_singular_slater_matrix(pimc):
-    # An up-spin electron 400 bohr from the trap centre on one slice: its
-    # SHONodes column exp(-c((r_i^2 + r_j^2) cosh - 2 r_i.r_j)) underflows to
-    # exactly 0, so LU meets an exactly zero pivot (dgetrf's info > 0, where
-    # pi-qmc prints "BAD RETURN" and, at a set-up, loops until it exits).  The
-    # engine stops that rescale loop at once: PIMC_STATUS_SINGULAR.
-    def bad(p):
-        q = p.copy()
-        q[5, 0] = [400.0, 0.0, 0.0]
-        return q
-    clean, broken = run_three(pimc, "dot4_fn", bad, 200)
-    assert clean["status"][1] == 0
-    assert broken["status"][1] & pimc.PIMC_STATUS_SINGULAR
-    assert np.all(np.isfinite(broken["energy"][[0, 2]]))
-    assert_others_unaffected(clean, broken)
