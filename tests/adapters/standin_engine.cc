@@ -177,6 +177,13 @@ int pimc_thermo_energy(pimc_engine* e, double* host_energy) {
   return PIMC_OK;
 }
 
+// Table building is the engine's own (host) code, not part of what the stand-in
+// computes; the tests that link it build engines from pi-qmc's tables.
+int pimc_coulomb_tables(const pimc_system*, int, int, double, double, double, double,
+                        const pimc_pair_table**, int*, const pimc_ewald_table**) {
+  return fail(PIMC_ERR_INVALID, "stand-in: no table builder");
+}
+
 // Counters for the test: node evaluations, action differences, scale changes.
 void standin_counts(pimc_engine* e, int* node, int* action, int* pushes) {
   *node = e->calls_node;

@@ -6,10 +6,14 @@ sources built from the reference tree) run in separate processes, each from
 its own seeded initial path and random stream: `equil` sweeps are discarded,
 then `nblock` blocks of `block` sweeps follow, the ThermoEnergyEstimator value
 (src/estimator/ThermoEnergyEstimator.cc:32-66) measured after every sweep (one
-sweep = ceil(M / 2^L) * N section attempts, pi-qmc's usual interval).  The file
-holds every block mean; E is their mean and sigma their standard error
-(PROCS * nblock >= 50 blocks, each far longer than the estimator's
-autocorrelation time).
+sweep = ceil(M / 2^L) * N section attempts, pi-qmc's usual interval).  Every
+sweep is followed by DISP rigid displacement attempts of one particle's whole
+path (DisplaceMoveSampler / DoubleDisplaceMoveSampler with a UniformMover of
+box DISP_BOX): bisection sections move a path's centroid only slowly, and
+without them the potential energy decorrelates over many thousands of sweeps
+(blocks of 1500 sweeps then understate the error).  The file holds every block
+mean; E is their mean and sigma their standard error (PROCS * nblock >= 50
+blocks).
 
 Usage: python tests/golden/make_energy.py [case ...]   (needs the reference tree)
 """
@@ -31,6 +35,7 @@ CASES = {
     "dot4_fn": ("dot4_fn", "const", 1000, 16, 500),
 }
 SEED = 5150
+DISP, DISP_BOX = 2, 1.0
 
 
 def sweep_attempts(kw):
@@ -50,15 +55,21 @@ def chain(args):
     ref.set_path(W.initial_path(cfg, init, seed=SEED + 17 * p))
     sw = sweep_attempts(kw)
     n = 0
-    for _ in range(equil):
+
+    def sweep():
+        nonlocal n
         ref.run(sw, first_attempt=n)
         n += sw
+        ref.run_displace(DISP, [DISP_BOX] * 3, 1, -1, first_attempt=n)
+        n += DISP
+
+    for _ in range(equil):
+        sweep()
     means = []
     for _ in range(nblock):
         e = 0.0
         for _ in range(block):
-            ref.run(sw, first_attempt=n)
-            n += sw
+            sweep()
             e += ref.thermo_energy()
         means.append(e / block)
     return means
@@ -72,7 +83,7 @@ def make(name):
     e, sig = float(flat.mean()), float(flat.std(ddof=1) / np.sqrt(flat.size))
     np.savez_compressed(os.path.join(HERE, "energy_" + name + ".npz"), block_means=means,
                         energy=e, sigma=sig, equil=equil, block=block, golden=golden,
-                        seed=SEED, init=init)
+                        seed=SEED, init=init, disp=DISP, disp_box=DISP_BOX)
     half = means[:, :nblock // 2].mean() - means[:, nblock // 2:].mean()
     print(f"energy_{name}: E = {e:.6f} +- {sig:.6f} ({flat.size} blocks of {block} sweeps "
           f"after {equil}); first half - second half = {half:+.5f}")

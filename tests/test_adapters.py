@@ -148,3 +148,46 @@ def test_adapters_reproduce_golden_records(adapter_check, tmp_path, case, n):
         assert energy == pytest.approx(g["energy1"], rel=1e-12)
     if case == "dot20_fn":
         assert counts[2] > 0  # pi-qmc's set-up rescaled the determinant: the scale followed
+
+
+def test_gpu_tags_parse_into_the_engine_system(tmp_path):
+    """<GpuAction> with pi-qmc's own action children (SpringAction, SHOAction,
+    PrimSHOAction, CoulombAction, FixedNodeAction with SHONodes) parsed by the
+    GPU tag parser on pi-qmc's XMLParser (compiled from the reference tree,
+    libxml2 replaced by a stand-in) into the engine's system; unknown tags and
+    a sampler mover that disagrees are refused; <GpuSample> builds the device
+    sampler."""
+    if not (os.path.isdir(os.path.join(REF, "src")) and
+            os.path.exists(os.path.join(REPO, "oracle", "_ref", "libpimcref.so"))):
+        pytest.skip("pi-qmc source tree and its compiled objects not present")
+    import oracle_lib
+    port = oracle_lib.build_port()
+    refdir = os.path.join(REPO, "oracle", "_ref")
+    exe = str(tmp_path / "parser_check")
+    cmd = ["g++", "-std=gnu++11", "-O1", "-w", "-DHAVE_CONFIG_H",
+           "-I" + os.path.join(REPO, "tests", "adapters", "stub_libxml"),
+           "-I" + os.path.join(REPO, "oracle", "shim"), "-I" + os.path.join(REF, "src"),
+           "-I" + os.path.join(REF, "contrib", "blitz-0.9"),
+           "-I" + os.path.join(REPO, "include"), "-I" + os.path.join(REPO, "oracle"),
+           "-I" + os.path.join(REPO, "pi-qmc_gb300", "adapters"),
+           os.path.join(REPO, "tests", "adapters", "parser_check.cc"),
+           os.path.join(REPO, "pi-qmc_gb300", "adapters", "GpuParser.cc"),
+           os.path.join(REPO, "pi-qmc_gb300", "adapters", "GpuAdapters.cc"),
+           os.path.join(REPO, "tests", "adapters", "standin_engine.cc"),
+           os.path.join(REF, "src", "parser", "XMLParser.cc"), "-o", exe,
+           "-L" + refdir, "-lpimcref", "-Wl,-rpath," + refdir, port,
+           "-Wl,-rpath," + os.path.dirname(port)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-3000:]
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    lines = [l for l in out.stdout.splitlines() if l and l[0].isdigit()]
+    v = lines[-3].split()
+    # npart nspecies counts sho_omega prim_a prim_a prim_b mass charge cell node_kind
+    # node_omega node_temperature nslice tau nlevel epsilon spring coulomb norder mover replicas
+    assert v[:12] == ["4", "2", "2", "2", "1", "1", "0", "0.5", "0.25", "1", "-1", "1000"]
+    assert v[12:17] == ["1", "1", "1.25", "1.5", "0.5"]
+    assert v[17] == "64" and float(v[18]) == 4.0 / 64 and v[19] == "3"
+    assert v[20:26] == ["2", "1", "1", "3", "0", "7"]
+    assert lines[-2] == "1"              # precision: mixed
+    assert lines[-1] == "2 1"            # both refusals, and a sampler

@@ -18,7 +18,8 @@
 
 Engine standard errors come from the spread of per-replica means over 512
 (1024 for the SHO test) independent replicas, each its own Markov chain,
-measured once per sweep after the same equilibration as the reference's.
+measured once per sweep after an equilibration, each sweep followed by the
+reference run's rigid displacement attempts.
 """
 import math
 
@@ -42,14 +43,29 @@ def sweep_attempts(kw):
     return -(-kw["nslice"] // (1 << kw["nlevel"])) * sum(kw["counts"])
 
 
-def equilibrated_energy(pimc, kw, tables, kind, precision, nrep, equil, measure, attempts):
+def equilibrated_energy(pimc, kw, tables, kind, precision, nrep, equil, measure, attempts,
+                        disp=0):
+    """Per-replica means over `measure` measurements after `equil` untimed
+    steps; a step is `attempts` section attempts and, with `disp`, that many
+    rigid displacement attempts of one particle's whole path in a 1-bohr box
+    (the protocol of tests/golden/make_energy.py)."""
     class _C:
         nslice, npart, cell = kw["nslice"], sum(kw["counts"]), [kw["cell"]] * 3
 
     e = pimc.Engine(kw, nrep, tables, None, seed=808, precision=precision)
     e.upload_paths([W.initial_path(_C, kind, seed=3000 + r) for r in range(nrep)])
-    e.run_steps(attempts, equil, energies=False)
-    E = e.run_steps(attempts, measure)  # [measure][nrep]
+    if disp:
+        for _ in range(equil):
+            e.run_sections(attempts)
+            e.run_displace(disp, [1.0, 1.0, 1.0], 1, -1)
+        E = np.empty((measure, nrep))
+        for k in range(measure):
+            e.run_sections(attempts)
+            e.run_displace(disp, [1.0, 1.0, 1.0], 1, -1)
+            E[k] = e.thermo_energy()
+    else:
+        e.run_steps(attempts, equil, energies=False)
+        E = e.run_steps(attempts, measure)  # [measure][nrep]
     acc, att, st = e.replica_status()
     e.close()
     assert np.all(st == 0) and np.all(np.isfinite(E))
@@ -77,7 +93,7 @@ def test_energy_matches_pi_qmc(pimc, case, kind, equil, measure, precision):
     ref = np.load(golden_io.GOLDEN + "/energy_" + case + ".npz")
     g = golden_io.load(case)
     e, sig = equilibrated_energy(pimc, g["kw"], g["tables"], kind, precision, 512, equil,
-                                 measure, sweep_attempts(g["kw"]))
+                                 measure, sweep_attempts(g["kw"]), disp=int(ref["disp"]))
     er, sr = float(ref["energy"]), float(ref["sigma"])
     assert ref["block_means"].size >= 50
     assert abs(e - er) <= 2 * math.hypot(sig, sr), (case, precision, e, sig, er, sr)
