@@ -62,6 +62,8 @@ def parse():
                    help="requests of the serving sub-run in the default line (0: none)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    p.add_argument("--launch", default="",
+                   help="block,scratch_global,regs_variant: this launch shape, no autotuning")
     p.add_argument("--requests", type=int, default=2000, help="serve: requests in the stream")
     p.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     p.add_argument("--sweep-scale", type=float, default=1e-5,
@@ -115,12 +117,19 @@ def sweep_attempts(kw):
 # counted on: another build's counts are not used (the line then falls back to
 # the operation-count model and says so).
 MEASURED_WORK = {
-    ("dot20_fn", "mixed"): dict(fp64=2.412e5, fp32=None, dram=1.123e5, sha="292ad9418616be78"),
-    ("dot20_fn", "fp64"): dict(fp64=4.790e5, fp32=None, dram=1.190e5, sha="292ad9418616be78"),
+    # launch shape of the count (block, scratch placement, register variant):
+    # the DRAM bytes depend on the scratch placement, the flops do not
+    ("dot20_fn", "mixed"): dict(fp64=3.423e5, fp32=1.692e5, dram=1.483e5, shape="256,0,2",
+                                sha="dcfada002f88efa7"),
+    ("dot20_fn", "fp64"): dict(fp64=6.504e5, fp32=4.475e3, dram=1.452e5, shape="256,0,2",
+                               sha="dcfada002f88efa7"),
     # counted on the first 1024 replicas of the mix
-    ("batch4096", "mixed"): dict(fp64=1.624e5, fp32=None, dram=3.723e4, sha="292ad9418616be78"),
-    ("heg54", "mixed"): dict(fp64=3.802e6, fp32=None, dram=2.037e6, sha="292ad9418616be78"),
-    ("dot2", "fp64"): dict(fp64=1.896e4, fp32=None, dram=613.5, sha="292ad9418616be78"),
+    ("batch4096", "mixed"): dict(fp64=1.569e5, fp32=7.441e4, dram=4.653e4, shape="128,2,2",
+                                 sha="dcfada002f88efa7"),
+    ("heg54", "mixed"): dict(fp64=1.906e6, fp32=4.791e5, dram=4.010e6, shape="512,2,1",
+                             sha="dcfada002f88efa7"),
+    ("dot2", "fp64"): dict(fp64=1.945e4, fp32=164.4, dram=497.4, shape="64,0,2",
+                           sha="dcfada002f88efa7"),
 }
 
 
@@ -505,15 +514,6 @@ def run_engine(args, rank, world):
     paths = np.concatenate([WL.initial_path(shape_of(systems[r]), init_kind(args.workload),
                                             seed=100 + r).ravel() for r in range(R)])
     eng.upload_paths(paths)
-    # launch configuration chosen by the autotuner (untimed; the chains are restored)
-    tuned, tried = eng.autotune(min(A, 32)) if not args.no_autotune else (eng.launch_config(), [])
-    # depth statistics for the flop model (untimed)
-    rec = eng.run_sections(4, records=True)
-    Ls = np.array([k["nlevel"] for k in systems])[:, None]
-    rl = rec["reject_level"]
-    depth_reach = [float(np.mean((rl < 0) | (rl <= Ls - d))) for d in range(int(Ls.max()) + 1)]
-    reach = [depth_reach[L - lev] for lev in range(L + 1)]
-    eng.upload_paths(paths)
     # equilibration (untimed): the energy block below is taken on equilibrated chains
     rounds, ndisp, nsweep = default_equil(args.workload)
     if args.equil >= 0:
@@ -523,6 +523,22 @@ def run_engine(args, rank, world):
             eng.run_displace(ndisp, [1.0, 1.0, 1.0], 1, -1)
         eng.run_steps(A, nsweep, energies=False)
     equil = rounds * nsweep
+    # launch configuration chosen by the autotuner on the equilibrated chains
+    # (untimed; the chains are restored after every trial)
+    if args.launch:
+        b, g, v = (int(x) for x in args.launch.split(","))
+        eng.configure(b, g, 0, v)
+        tuned, tried = eng.launch_config(), []
+    elif args.no_autotune:
+        tuned, tried = eng.launch_config(), []
+    else:
+        tuned, tried = eng.autotune(min(A, 32))
+    # depth statistics for the flop model (untimed; the chains continue)
+    rec = eng.run_sections(4, records=True)
+    Ls = np.array([k["nlevel"] for k in systems])[:, None]
+    rl = rec["reject_level"]
+    depth_reach = [float(np.mean((rl < 0) | (rl <= Ls - d))) for d in range(int(Ls.max()) + 1)]
+    reach = [depth_reach[L - lev] for lev in range(L + 1)]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         eng.run_steps(A, 1, energies=False)
@@ -762,6 +778,7 @@ def section_roofline(args, systems, batch, kw, R, A, reach, depth_reach, section
            "frac": achieved / fp64_peak, "traffic": traffic, "kernel": "section_moves_kernel",
            "section_ms_per_launch": section_ms, "flops_per_launch": flops,
            "flops_source": source, "count_stale": stale, "kernel_sha": sha,
+           "count_launch_shape": work.get("shape") if work else None,
            "peak_source": "measured FP64 FMA probe (pimc_fp64_peak); MEASURED_PEAKS.json holds "
                           "no FP64 figure",
            "flops_per_attempt_model": attempt_flops(kw, reach), "level_reach": reach}

@@ -126,6 +126,8 @@ struct pimc_engine {
   DevBuf<long long> d_ekcache;  // structure factors per replica and slice
   DevBuf<long long> d_ekstage;  // per-CTA staging of an attempt's new structure factors
   int ekstage_stride = 0;       // int64 words per CTA
+  DevBuf<double> d_xstage;      // mixed form: per-CTA staging of changed slices' inverses
+  long long xstage_cta = 0;     // doubles per CTA
   DevBuf<int> d_order;
   DevBuf<int> d_next;
   DevBuf<double> d_ugrid;
@@ -178,6 +180,7 @@ struct pimc_engine {
     d_ekcache.free();
     d_prefill_scr.free();
     d_ekstage.free();
+    d_xstage.free();
     d_order.free();
     d_next.free();
     d_pool.free();
@@ -337,7 +340,30 @@ int cache_entry_doubles(const DevSys& d) {
   bool free_nodes = false;
   for (int i = 0; i < d.nspecies; ++i) free_nodes |= d.node_kind[i] == PIMC_NODES_FREE;
   const int n = d.ns_max;
-  return (2 + 2 * n + n * n * (free_nodes ? 4 : 1) + 2) & ~1;  // + the stale-row word
+  // + the stale-row word; the mixed form adds, for free-particle nodes, the
+  // inverse block (epoch, update count, n*n inverse) that its Sherman-Morrison
+  // updates work on (sm_species)
+  const bool xblock = d.mixed && free_nodes;
+  return (2 + 2 * n + n * n * (free_nodes ? 4 : 1) + 1 + (xblock ? 2 + n * n : 0) + 1) & ~1;
+}
+
+// Doubles of inverse-block staging one CTA needs for a replica (mixed form with
+// a cache and free-particle nodes).
+long long xstage_doubles(const DevSys& d) {
+  bool free_nodes = false;
+  for (int i = 0; i < d.nspecies; ++i) free_nodes |= d.node_kind[i] == PIMC_NODES_FREE;
+  return d.mixed && free_nodes && d.nc_offset >= 0
+             ? (long long)d.nsec * (d.ns_max * d.ns_max + 2)
+             : 0;
+}
+
+// Grows the inverse-block staging to grid CTAs of e->xstage_cta doubles.
+int ensure_xstage(pimc_engine* e, int grid) {
+  const size_t need = (size_t)grid * e->xstage_cta;
+  if (need == 0 || need <= e->d_xstage.n) return PIMC_OK;
+  CU(cudaStreamSynchronize(e->stream));
+  if (e->d_xstage.alloc(need)) return fail(PIMC_ERR_CUDA, "cudaMalloc inverse staging");
+  return PIMC_OK;
 }
 
 // Fixed-point exponent of a replica's structure-factor cache, or -1 when it
@@ -695,6 +721,11 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
         return fail(PIMC_ERR_CUDA, "cudaMalloc node cache");
       }
       cudaMemset(e->d_nodecache.p, 0xff, coff * sizeof(double));  // NaN epochs: all invalid
+    }
+    for (const DevSys& d : e->hsys) e->xstage_cta = std::max(e->xstage_cta, xstage_doubles(d));
+    if (e->xstage_cta > 0 && e->d_xstage.alloc((size_t)e->grid * e->xstage_cta)) {
+      delete e;
+      return fail(PIMC_ERR_CUDA, "cudaMalloc inverse staging");
     }
   }
   // Structure-factor cache of Ewald systems (left out, like the Slater cache,
@@ -1076,6 +1107,8 @@ void fill_run_params(pimc_engine* e, RunParams& P, int nattempt, pimc_move_recor
   P.ekcache = e->d_ekcache.p;
   P.ekstage = e->d_ekstage.p;
   P.ekstage_stride = e->ekstage_stride;
+  P.xstage = e->xstage_cta > 0 ? e->d_xstage.p : nullptr;
+  P.xstage_cta = e->xstage_cta;
   P.rec = d_rec;
   P.order = e->d_order.p;
   P.next = e->d_next.p;
@@ -1557,6 +1590,7 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
     if (e->d_ekstage.alloc((size_t)grid * e->ekstage_stride))
       return fail(PIMC_ERR_CUDA, "cudaMalloc structure-factor staging");
   }
+  if (int rc = ensure_xstage(e, grid)) return rc;
   e->lay = L;
   e->lay_opts = opts;
   e->ctas_cap = ctas_cap;
@@ -1678,8 +1712,10 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   if (ntried) *ntried = nt;
   int rc;
   if (ibest >= 0) {
+    // the placement the trial ran: 1 all scratch global, 2 only its cold part
     LayoutOpts o;
-    o.scratch_global = cand[ibest].scratch_global != 0;
+    o.scratch_global = cand[ibest].scratch_global == 1;
+    o.cold_global = cand[ibest].scratch_global == 2;
     rc = apply_config(e, cand[ibest].block, o, cand[ibest].ctas_per_sm, cand[ibest].regs_variant);
     *best = cand[ibest];
   } else {
@@ -1749,6 +1785,7 @@ int refresh_order(pimc_engine* e) {
     int occ = 1;
     occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
     e->grid = std::min(e->nactive, e->num_sms * std::max(occ, 1));
+    if (int rc = ensure_xstage(e, e->grid)) return rc;
     if (e->lay.gcta > 0) {
       const size_t need = (size_t)e->grid * e->lay.gcta;
       if (need > e->d_nodescr.n) {
@@ -1811,6 +1848,8 @@ int pimc_server_create(const pimc_server_config* cfg, uint64_t seed, int precisi
   set_smem_caps();
   e->lay = biggest;
   e->grid = std::min(cfg->slots, nsm);
+  if (precision == PIMC_PREC_MIXED && mx.fixed_node)
+    e->xstage_cta = (long long)mx.nsec * (mx.ns_max * mx.ns_max + 2);
   const long long words = (long long)(cfg->hbm_bytes / sizeof(double));
   if (e->d_pool.alloc(words) || e->d_sys.alloc(cfg->slots) || e->d_state.alloc(cfg->slots) ||
       e->d_order.alloc(cfg->slots) || e->d_next.alloc(1) || e->d_slot_attempts.alloc(cfg->slots) || e->d_ugrid.alloc(1 << 22) ||
@@ -1845,6 +1884,7 @@ int pimc_server_admit(pimc_engine* e, const pimc_system* sys, const pimc_pair_ta
   if (r < 0) return fail(PIMC_ERR_CAPACITY, "no free slot");
   const long long pw = 3LL * sys->nslice * sys->npart;
   const bool cache = d.fixed_node && (1 << d.nlevel) < d.nslice / 2;
+  d.mixed = e->precision == PIMC_PREC_MIXED;
   d.nc_stride = cache_entry_doubles(d);
   const long long cw = cache ? (long long)d.nspecies * d.nslice * d.nc_stride : 0;
   const long long po = pool_alloc(e, pw + cw);
@@ -1971,6 +2011,8 @@ int pimc_server_run(pimc_engine* e) {
   P.ekcache = nullptr;  // servers take no Ewald systems
   P.ekstage = nullptr;
   P.ekstage_stride = 0;
+  P.xstage = e->xstage_cta > 0 ? e->d_xstage.p : nullptr;
+  P.xstage_cta = e->xstage_cta;
   P.rec = nullptr;
   P.order = e->d_order.p;
   P.next = e->d_next.p;

@@ -37,14 +37,20 @@ struct RunParams {
   long long* ekcache;     // structure-factor cache pool (null: none)
   long long* ekstage;     // per-CTA staging of an attempt's new structure factors
   int ekstage_stride;     // int64 words per CTA
+  double* xstage;         // mixed form: per-CTA staging of changed slices' inverses (null: none)
+  long long xstage_cta;   // doubles per CTA
   int nrep;
   uint64_t seed;
   Layout lay;
 };
 
 __device__ __forceinline__ Smem carve(double* base, const Layout& L, const DevSys& s,
-                                      double* nodescr_g) {
+                                      double* nodescr_g, double* xstage = nullptr) {
   Smem m;
+  // mixed form: this CTA's staging of the inverse blocks of an attempt's changed
+  // slices ([nsec][2 + ns_max^2], global memory), committed to the cache on accept
+  m.xstage = xstage;
+  m.xstage_stride = s.ns_max * s.ns_max + 2;
   const int ss = s.nsec * s.npart;
   m.s1x = base + L.s1;
   m.s1y = m.s1x + ss;
@@ -319,16 +325,31 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
                                                    double& det, int& err, double* d1,
                                                    double* d2, double* newcol = nullptr,
                                                    unsigned rowmask = 0xffffffffu,
-                                                   double* cold = nullptr) {
-  if (W == 8)
+                                                   double* cold = nullptr,
+                                                   const double* xin = nullptr,
+                                                   double det_in = 0.0, double* xout = nullptr,
+                                                   double xepoch = 0.0) {
+  // (xin and xout are the same for every lane of a warp)
+  if (xin || xout) {
+    if (W == 8)
+      node_eval_group<8, true>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err,
+                               d1, d2, newcol, rowmask, cold, xin, det_in, xout, xepoch);
+    else if (W == 16)
+      node_eval_group<16, true>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err,
+                                d1, d2, newcol, rowmask, cold, xin, det_in, xout, xepoch);
+    else
+      node_eval_group<32, true>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err,
+                                d1, d2, newcol, rowmask, cold, xin, det_in, xout, xepoch);
+  } else if (W == 8) {
     node_eval_group<8>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
                        newcol, rowmask, cold);
-  else if (W == 16)
+  } else if (W == 16) {
     node_eval_group<16>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
                         newcol, rowmask, cold);
-  else
+  } else {
     node_eval_group<32>(s, sp, v1, v2, scale, scr, full, ecache, jcol, write, det, err, d1, d2,
                         newcol, rowmask, cold);
+  }
 }
 
 // Index of the entry's stale-row word (after the element matrices): bit r set
@@ -337,6 +358,19 @@ __device__ __forceinline__ void node_eval_dispatch(int W, const DevSys& s, int s
 __device__ __forceinline__ int cache_mask_slot(const DevSys& s, int sp) {
   const int n = s.spec_count[sp];
   return 2 + 2 * n + n * n * (s.node_kind[sp] == PIMC_NODES_FREE ? 4 : 1);
+}
+// Whether a species' cached Slater entries carry the inverse block that the
+// mixed form's Sherman-Morrison updates work on: FreeParticleNodes species.
+// (The SHONodes matrices of the cold dots are ill-conditioned by
+// construction, cond 1e12..1e14 at omega/T = 20, where every factorisation
+// fails the updates' conditioning gate: the block would only cost them.)
+__host__ __device__ __forceinline__ bool sm_species(const DevSys& s, int sp) {
+  return s.mixed && s.node_kind[sp] == PIMC_NODES_FREE;
+}
+// Mixed form: index of the entry's inverse block [epoch of its scale, updates
+// since the last factorisation, inverse (n*n, X layout)], after the stale-row word.
+__device__ __forceinline__ int cache_x_slot(const DevSys& s, int sp) {
+  return cache_mask_slot(s, sp) + 1;
 }
 __device__ __forceinline__ unsigned cache_rowmask(const double* e, int slot) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(e[slot]);
@@ -422,8 +456,10 @@ static __device__ __noinline__ void node_init_pass(const DevSys& s, const Smem& 
     double* d1 = mine ? m.dist + (t * 2) * nsm : (e ? e + 2 : nullptr);
     double* d2 = mine ? m.dist + (t * 2 + 1) * nsm : (e ? e + 2 + n : nullptr);
     const unsigned rmask = e ? cache_rowmask(e, cache_mask_slot(s, sp)) : 0xffffffffu;
+    // mixed form: the entry's inverse, updated for its changed rows when it can be
+    double* xb = (e && sm_species(s, sp)) ? e + cache_x_slot(s, sp) : nullptr;
     node_eval_dispatch(W, s, sp, v1, v2, scale[sp], scrm, full, ec, -1, act, det, err, d1, d2,
-                       nullptr, rmask, coldm);
+                       nullptr, rmask, coldm, xb, e ? e[1] : 0.0, xb, (double)epoch[sp]);
     if (act) {
       if (e && mine && glm < n) {
         e[2 + glm] = d1[glm];
@@ -540,7 +576,7 @@ static __device__ __noinline__ void node_initialize(const DevSys& s, const Smem&
 // FixedNodeAction::getActionDifference (src/fixednode/FixedNodeAction.cc:39-131)
 // for the moving species at one level.
 static __device__ __noinline__ double node_level(const DevSys& s, const Smem& m, double scale, int msp, int ipart,
-                             int level, double* cache, int ifirst1) {
+                             int level, double* cache, int ifirst1, int ep) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max;
   const int nStride = 1 << (level + 1);
@@ -577,13 +613,22 @@ static __device__ __noinline__ double node_level(const DevSys& s, const Smem& m,
     double det = 0;
     int err = 0;
     double* ec = nullptr;
-    if (cache)
-      ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
-    else if (sho && m.ecache)
+    const double* xb = nullptr;  // mixed form: the entry's inverse block
+    double det_in = 0.0;
+    if (cache) {
+      double* e = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice));
+      ec = e + 2 + 2 * n;
+      if (sm_species(s, msp) && m.xstage) {
+        xb = e + cache_x_slot(s, msp);
+        det_in = e[1];
+      }
+    } else if (sho && m.ecache) {
       ec = m.ecache + (size_t)t * n * n;
+    }
     node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
                        m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
+                       cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold, xb, det_in,
+                       xb ? m.xstage + (size_t)t * m.xstage_stride : nullptr, (double)ep);
     if (act && (lane & (W - 1)) == 0) {
       m.ndm[t] = det;
       if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1);
@@ -640,7 +685,7 @@ __device__ __forceinline__ uint32_t level_uniform_base(const DevSys& s, int leve
 // The caller applies pi-qmc's level-by-level decisions to them.
 static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, double scale, int msp,
                                   int ipart, int lo, int hi, bool mynode, double* cache,
-                                  int ifirst1, uint64_t seed, uint32_t att, double* lds,
+                                  int ifirst1, int ep, uint64_t seed, uint32_t att, double* lds,
                                   double* llt, double* lnd) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
@@ -694,13 +739,22 @@ static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, d
       double det = 0;
       int err = 0;
       double* ec = nullptr;
-      if (cache)
-        ec = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice)) + 2 + 2 * n;
-      else if (sho && m.ecache)
+      const double* xb = nullptr;  // mixed form: the entry's inverse block
+      double det_in = 0.0;
+      if (cache) {
+        double* e = cache_entry(s, cache, msp, wrap_slice(ifirst1 + t, s.nslice));
+        ec = e + 2 + 2 * n;
+        if (sm_species(s, msp) && m.xstage) {
+          xb = e + cache_x_slot(s, msp);
+          det_in = e[1];
+        }
+      } else if (sho && m.ecache) {
         ec = m.ecache + (size_t)t * n * n;
+      }
       node_eval_dispatch(W, s, msp, v1, v2, scale, scr, 1, ec, jcol, act, det, err,
                          m.ndist + (t * 2) * nsm, m.ndist + (t * 2 + 1) * nsm,
-                         cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold);
+                         cache ? m.ncol + t * m.ncol_stride : nullptr, 0u, cold, xb, det_in,
+                         xb ? m.xstage + (size_t)t * m.xstage_stride : nullptr, (double)ep);
       if (act && (lane & (W - 1)) == 0) {
         m.ndm[t] = det;
         if (err || det * m.dm[msp * nsec + 0] <= 1e-200) atomicOr(&m.ictl[C_FLAG], 1 << l);
@@ -764,7 +818,8 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         dst[i] = src[i];
     }
     if (threadIdx.x == 0) {
-      M_ = carve(smem, P.lay, P.sys[r], P.nodescr_g);
+      M_ = carve(smem, P.lay, P.sys[r], P.nodescr_g,
+                 P.xstage ? P.xstage + (size_t)blockIdx.x * P.xstage_cta : nullptr);
       status = P.state[r].status;
       nacc = 0;
       for (int k = 0; k < kMaxSpecies; ++k) {
@@ -837,8 +892,8 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         double* lds = m.red + kWarps + 8;  // [kMaxLevels] per level: action difference,
         double* llt = lds + kMaxLevels;     // mover ln T,
         double* lnd = llt + kMaxLevels;     // fixed-node difference
-        top_levels(s, m, scale[msp], msp, ipart, lb, L, mynode, cache, ifirst1, P.seed, att, lds,
-                   llt, lnd);
+        top_levels(s, m, scale[msp], msp, ipart, lb, L, mynode, cache, ifirst1, epoch[msp], P.seed,
+                   att, lds, llt, lnd);
         __syncthreads();
         if (threadIdx.x < 32) {
           // Lane i takes level L - i: every level's acceptance probability
@@ -894,7 +949,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
             for (int t = 1; t < nsec - 1; ++t) ds += ewald_slice_diff(s, m, ipart, t);
         }
         double dsn = 0.0;
-        if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level, cache, ifirst1);
+        if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level, cache, ifirst1, epoch[msp]);
         if (threadIdx.x == 0) {
           const double total = s.fixed_node ? ds + dsn : ds;
           const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
@@ -948,6 +1003,15 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
             e[2 + 2 * n + jcol * n + j] = nc[j];
             if (!sho)
               for (int c = 1; c < 4; ++c) e[2 + 2 * n + c * n * n + jcol * n + j] = nc[c * n + j];
+          }
+          if (sm_species(s, msp) && m.xstage) {
+            // the moved slices' inverse blocks, as the level evaluations left them
+            const int xw = n * n + 2, xs = cache_x_slot(s, msp);
+            for (int it = threadIdx.x; it < (nsec - 2) * xw; it += blockDim.x) {
+              const int k = 1 + it / xw, w = it - (k - 1) * xw;
+              cache_entry(s, cache, msp, wrap_slice(ifirst1 + k, M))[xs + w] =
+                  m.xstage[(size_t)k * m.xstage_stride + w];
+            }
           }
           __syncthreads();
           for (int k = 1 + threadIdx.x; k < nsec - 1; k += blockDim.x) {

@@ -92,8 +92,15 @@ __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) 
     SliceView v2{st + 3 * n - f, st + 4 * n - f, st + 5 * n - f, n, 0, -1, 0, 0, 0};
     double det = 0;
     int err = 0;
-    node_eval_group<32>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err, e + 2,
-                        e + 2 + n, nullptr, 0xffffffffu, cold);
+    // (mixed form, free-particle nodes: the inverse block too, the start of
+    // its update count)
+    if (sm_species(s, sp))
+      node_eval_group<32, true>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err,
+                                e + 2, e + 2 + n, nullptr, 0xffffffffu, cold, nullptr, 0.0,
+                                e + cache_x_slot(s, sp), ep);
+    else
+      node_eval_group<32>(s, sp, v1, v2, scale, scr, 1, e + 2 + 2 * n, -1, true, det, err, e + 2,
+                          e + 2 + n, nullptr, 0xffffffffu, cold);
     __syncwarp();
     if (lane == 0) {
       e[1] = det;

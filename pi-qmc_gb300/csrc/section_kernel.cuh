@@ -40,6 +40,8 @@ struct Smem {
   double* nodecold;         // cold parts of the node scratch when apart (global), or null
   int nodecold_stride;      // doubles per warp
   int ewt_cols;             // bead columns of the Ewald tables area
+  double* xstage;           // mixed form: [nsec][xstage_stride] inverse blocks (global), or null
+  int xstage_stride;
 };
 
 
@@ -74,6 +76,15 @@ struct SliceView {
 };
 
 // ------------------------------------------------------------------ node model
+// The mixed form's Sherman-Morrison updates of cached inverses: at most
+// kSmRefresh updates between two factorisations of a slice pair's matrix, and
+// none whose determinant ratio is below kSmMinRatio in magnitude.
+// A factorisation whose conditioning estimate n max|a| max|inv| exceeds
+// kSmMaxCond starts no updates: an update's relative error grows with the
+// condition number (the SHONodes matrices of a cold dot reach 1e13 and more).
+constexpr double kSmRefresh = 16.0;
+constexpr double kSmMinRatio = 0.05;
+constexpr double kSmMaxCond = 1e7;
 // Scratch doubles one lane group needs for an n-particle species: a hot part
 // (the LU and the inverse, rewritten at every elimination step, and the
 // reciprocal pivots) and a cold part (the SHO exp matrix, or the free-particle
@@ -109,13 +120,18 @@ __device__ __forceinline__ double* group_cold(const Smem& m, int warp, int g, in
 // nothing.  For SHONodes, ecache (n*n, or null) holds the slice's exp matrix:
 // jcol < 0 fills it, jcol >= 0 reuses it and recomputes column jcol only (the
 // other columns' inputs are unchanged, so the values are bit-identical).
-template <int W>
+// kSm: the variant with the mixed form's Sherman-Morrison updates and inverse
+// blocks (xin / xout); without it those arguments are ignored and the
+// evaluation is the plain factorisation.
+template <int W, bool kSm = false>
 static __device__ __noinline__ void node_eval_group(const DevSys& s, int sp, const SliceView& v1,
                                 const SliceView& v2, double scale, double* scr, int full,
                                 double* ecache, int jcol, bool write, double& det_out,
                                 int& err_out, double* d1, double* d2,
                                 double* newcol = nullptr, unsigned rowmask = 0xffffffffu,
-                                double* cold = nullptr) {
+                                double* cold = nullptr, const double* xin = nullptr,
+                                double det_in = 0.0, double* xout = nullptr,
+                                double xepoch = 0.0) {
   constexpr unsigned FULL = 0xffffffffu;
   const int gl = threadIdx.x & (W - 1);
   const int n = s.spec_count[sp];
@@ -213,8 +229,95 @@ static __device__ __noinline__ void node_eval_group(const DevSys& s, int sp, con
     element(__ffs(rm) - 1, e % n);
   }
   __syncwarp();
-  // --- LU with partial pivoting (the pivot is the first largest |a|)
   int info = 0;
+  // --- the mixed form: Sherman-Morrison updates of the cached inverse (xin:
+  // its [epoch, updates, inverse] block) instead of a factorisation, for the
+  // new column jcol of a level evaluation or each changed row of a refresh.
+  // A group updates when its block is of the current scale (epoch), has had
+  // fewer than kSmRefresh updates since its last factorisation, and every
+  // determinant ratio is at least kSmMinRatio in magnitude (a refresh: at most
+  // n/2 rows); otherwise, or when another writing group of the warp cannot,
+  // the warp factorises as below.  Every lane takes part in the shuffles.
+  bool use_sm = false;
+  bool good = kSm && xin != nullptr && xin[0] == xepoch && xin[1] < kSmRefresh;
+  // (a warp none of whose writing groups can update factorises at once)
+  if (kSm && __any_sync(FULL, good && write) && __all_sync(FULL, good || !write)) {
+    const double* xc = good ? xin + 2 : nullptr;
+    for (int k = gl; k < nn; k += W) X[k] = xc ? xc[k] : 0.0;
+    __syncwarp();
+    double det = det_in;
+    if (jcol >= 0) {
+      // column jcol replaced by u = A(:, jcol): w = inv u, ratio = w_jcol,
+      // inv'(a, b) = inv(a, b) - (w_a - [a = jcol]) inv(jcol, b) / ratio
+      double w = 0.0;
+      if (gl < n)
+        for (int i = 0; i < n; ++i) w = __fma_rn(X[i * n + gl], A[jcol * n + i], w);
+      const double ratio = __shfl_sync(FULL, w, jcol, W);
+      good = good && fabs(ratio) >= kSmMinRatio;
+      use_sm = __all_sync(FULL, good || !write);
+      if (use_sm) {
+        const double rj = gl < n ? X[gl * n + jcol] : 0.0;  // inv(jcol, b), b = gl
+        const double f = gl < n ? (w - (gl == jcol ? 1.0 : 0.0)) / ratio : 0.0;
+        __syncwarp();
+        for (int e0 = 0; e0 < nn; e0 += W) {
+          const int e = e0 + gl;
+          const bool on = e < nn;
+          const int b = on ? e / n : 0, a = on ? e - b * n : 0;
+          const double fa = __shfl_sync(FULL, f, a, W);
+          const double rb = __shfl_sync(FULL, rj, b, W);
+          if (on) X[b * n + a] = __fma_rn(-fa, rb, X[b * n + a]);
+        }
+        det = __dmul_rn(det_in, ratio);
+      }
+    } else {
+      // each changed row i in turn, v = A(i, :): z = v inv, ratio = z_i,
+      // inv'(a, b) = inv(a, b) - inv(a, i) (z_b - [b = i]) / ratio
+      const int nr = __popc(rows_new);
+      good = good && nr > 0 && 2 * nr <= n;
+      const unsigned nrmax = __reduce_max_sync(FULL, good ? (unsigned)nr : 0u);
+      unsigned rm = good ? rows_new : 0u;
+      for (unsigned k = 0; k < nrmax; ++k) {
+        const bool live = rm != 0u;
+        const int i = live ? __ffs(rm) - 1 : 0;
+        rm &= rm - 1u;
+        double z = 0.0;
+        if (gl < n)
+          for (int j = 0; j < n; ++j) z = __fma_rn(A[j * n + i], X[gl * n + j], z);
+        const double ratio = __shfl_sync(FULL, z, i, W);
+        const double ci = gl < n ? X[i * n + gl] : 0.0;  // inv(a, i), a = gl
+        const double g = gl < n ? (z - (gl == i ? 1.0 : 0.0)) / ratio : 0.0;
+        __syncwarp();
+        for (int e0 = 0; e0 < nn; e0 += W) {
+          const int e = e0 + gl;
+          const bool on = e < nn && live;
+          const int b = e < nn ? e / n : 0, a = e < nn ? e - b * n : 0;
+          const double ca = __shfl_sync(FULL, ci, a, W);
+          const double gb = __shfl_sync(FULL, g, b, W);
+          if (on) X[b * n + a] = __fma_rn(-ca, gb, X[b * n + a]);
+        }
+        __syncwarp();
+        if (live) {
+          det = __dmul_rn(det, ratio);
+          good = good && fabs(ratio) >= kSmMinRatio;
+        }
+      }
+      use_sm = __all_sync(FULL, good || !write);
+    }
+    if (use_sm && write) {
+      det_out = det;
+      err_out = 0;
+    }
+  }
+  double amax = 0.0;  // max |a| of the matrix, for the conditioning estimate (mixed form)
+  // every lane takes part in the shuffles
+  const bool xany = kSm && __any_sync(FULL, xout != nullptr);
+  if (!use_sm) {
+  if (xany) {
+    for (int k = gl; k < nn; k += W) amax = fmax(amax, fabs(A[k]));
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(FULL, amax, o, W));
+  }
+  // --- LU with partial pivoting (the pivot is the first largest |a|)
   unsigned pivbits = 0;  // bit j set: row j was interchanged
   int piv_lane = gl;     // piv[gl] for gl < n
   for (int j = 0; j < n; ++j) {
@@ -343,6 +446,25 @@ static __device__ __noinline__ void node_eval_group(const DevSys& s, int sp, con
       }
     }
     __syncwarp();
+  }
+  }  // factorisation
+  // the inverse and its update count for the cache (mixed form); a fresh
+  // factorisation that is too ill-conditioned is marked as used up
+  if (xany) {
+    double xmax = 0.0;
+    if (!use_sm) {
+      for (int k = gl; k < nn; k += W) xmax = fmax(xmax, fabs(X[k]));
+#pragma unroll
+      for (int o = W / 2; o > 0; o >>= 1) xmax = fmax(xmax, __shfl_xor_sync(FULL, xmax, o, W));
+    }
+    if (write && xout) {
+      for (int k = gl; k < nn; k += W) xout[2 + k] = X[k];
+      if (gl == 0) {
+        xout[0] = info == 0 ? xepoch : __longlong_as_double(0x7ff8000000000000LL);
+        xout[1] = use_sm ? xin[1] + 1.0
+                         : (n * amax * xmax <= kSmMaxCond ? 0.0 : kSmRefresh);
+      }
+    }
   }
   // --- nodal distances: d = sqrt(2m / (tau |grad ln det|^2)), the gradient
   // with respect to r1_j (d1) and r2_i (d2); inv(j,i) = X[i*n + j].  (No early

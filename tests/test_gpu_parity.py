@@ -400,7 +400,10 @@ def test_autotune_does_not_advance_chains(pimc):
     assert best["ms"] > 0 and best["ms"] == min(t["ms"] for t in tried if t["ms"] > 0)
     acc, att, st = a.replica_status()
     assert att.sum() == 0
-    assert a.launch_config()["block"] == best["block"]
+    # the engine runs the shape the tuner reports (scratch placement included)
+    applied = a.launch_config()
+    assert all(applied[k] == best[k]
+               for k in ("block", "scratch_global", "ctas_per_sm", "regs_variant")), (applied, best)
     b.configure(best["block"], best["scratch_global"], best["ctas_per_sm"], best["regs_variant"])
     ra = a.run_sections(40, records=True)
     rb = b.run_sections(40, records=True)
@@ -467,17 +470,21 @@ def test_displace_matches_golden(pimc, case):
     assert np.abs(e.download_paths()[0] - d["path"]).max() <= 1e-12
 
 
-@pytest.mark.parametrize("case", ["dot4_fn", "dot2_full", "heg8"])
+@pytest.mark.parametrize("case", ["dot4_fn", "dot2_full", "heg8", "heg16_hot", "dot20_fn"])
 def test_mixed_form_on_identical_proposals(pimc, case):
     # Both precision forms draw the same FP64 proposals, so a mixed chain follows
     # the FP64 chain until a uniform falls within the mixed error of its
     # acceptance probability.  On the common attempts: ln T bit for bit (the
     # mover is FP64 in both), action differences (FP32 terms, compensated sums)
-    # within 1e-4 of max(|dS|, 1), fixed-node differences within 1e-4 of
-    # max(|dS_node|, 1); the thermodynamic estimator on identical paths within
+    # within 1e-4 of max(|dS|, 1), fixed-node differences (the mixed form
+    # takes determinant ratios from cached inverses above level 0 and follows
+    # moves by Sherman-Morrison updates between factorisations) within 1e-4 of
+    # max(|dS_node|, 1) — 2e-3 on the ill-conditioned config-2 dot, its FP64
+    # conditioning bar; the thermodynamic estimator on identical paths within
     # 1e-5 relative.
     g = golden_io.load(case)
-    n, R = 150, 8
+    tol = NODE_TOL.get(case, 1e-4)
+    n, R = (150, 8) if case != "dot20_fn" else (60, 4)
     out = []
     for prec in (1, 0):
         e = pimc.Engine(g["kw"], R, g["tables"], g["ewald"], seed=515, precision=prec)
@@ -500,7 +507,7 @@ def test_mixed_form_on_identical_proposals(pimc, case):
             fn = np.abs(f["ds_node"][r, a, lv]) < 1e99
             assert np.array_equal(np.abs(m["ds_node"][r, a, lv]) >= 1e99, ~fn)
             assert np.all(np.abs(m["ds_node"][r, a, lv] - f["ds_node"][r, a, lv])[fn]
-                          <= 1e-4 * np.maximum(np.abs(f["ds_node"][r, a, lv][fn]), 1.0))
+                          <= tol * np.maximum(np.abs(f["ds_node"][r, a, lv][fn]), 1.0))
         same &= ok
     assert compared >= n * R // 2
     em.upload_paths(ef.download_paths())
