@@ -326,6 +326,7 @@ void fill_sys(const pimc_system& s, DevSys& d) {
     d.rcut2 = (d.rcut2 > l2) ? l2 : d.rcut2;
   }
   d.rcut2 *= 0.25;
+  d.rcut2_lo = (float)(d.rcut2 * (1.0 - 1e-5));
   d.spring = s.spring;
   d.coulomb = s.coulomb;
   d.ewald = s.ewald;

@@ -48,6 +48,7 @@ struct DevSys {
   // a |r1 - r0|^2 + b r0.r1, a = (m / 2 tau') (x coth x - 1), b = m w tanh(x / 2), x = w tau'
   float sho_a[kMaxLevels][kMaxSpecies], sho_b[kMaxLevels][kMaxSpecies];
   double cell[3], cellb[3], rcut2;
+  float rcut2_lo;  // the mixed form's FP32 pre-test of pbc (pbc_f): rcut2 (1 - 1e-5)
   int spring, coulomb, ewald, mover, fixed_node;
   int mixed;  // PIMC_PREC_MIXED: pair-action terms in FP32, accumulated in FP64
   double epsilon;
@@ -99,6 +100,25 @@ __device__ __forceinline__ void pbc(const DevSys& s, double& x, double& y, doubl
     x = __dsub_rn(x, __dmul_rn(s.cell[0], ix));
     y = __dsub_rn(y, __dmul_rn(s.cell[1], iy));
     z = __dsub_rn(z, __dmul_rn(s.cell[2], iz));
+  }
+}
+
+// The mixed form's minimum image of an FP64 difference, rounded to FP32 for
+// its FP32 terms: pbc()'s decision taken in FP32 first, against rcut2 less
+// 1e-5 relative (the FP32 sum of three rounded squares errs by under 5e-7
+// relative, all terms positive), so every vector pbc() would image passes
+// the pre-test and then takes pbc()'s own FP64 test and image; the others
+// skip its FP64 dot product.
+__device__ __forceinline__ void pbc_f(const DevSys& s, double x, double y, double z, float& fx,
+                                      float& fy, float& fz) {
+  fx = (float)x;
+  fy = (float)y;
+  fz = (float)z;
+  if (fx * fx + fy * fy + fz * fz > s.rcut2_lo) {
+    pbc(s, x, y, z);
+    fx = (float)x;
+    fy = (float)y;
+    fz = (float)z;
   }
 }
 

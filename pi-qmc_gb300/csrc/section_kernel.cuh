@@ -771,12 +771,9 @@ static __device__ __noinline__ double action_partial_mixed(const DevSys& s, cons
       const double o1x = m.s1x[t1 * np + ipart], o1y = m.s1y[t1 * np + ipart], o1z = m.s1z[t1 * np + ipart];
       const double o0x = m.s1x[t0 * np + ipart], o0y = m.s1y[t0 * np + ipart], o0z = m.s1z[t0 * np + ipart];
       if (s.spring) {
-        double dx = n1x - n0x, dy = n1y - n0y, dz = n1z - n0z;
-        pbc(s, dx, dy, dz);
-        double ex = o1x - o0x, ey = o1y - o0y, ez = o1z - o0z;
-        pbc(s, ex, ey, ez);
-        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-        const float gx = (float)ex, gy = (float)ey, gz = (float)ez;
+        float fx, fy, fz, gx, gy, gz;
+        pbc_f(s, n1x - n0x, n1y - n0y, n1z - n0z, fx, fy, fz);
+        pbc_f(s, o1x - o0x, o1y - o0y, o1z - o0z, gx, gy, gz);
         acc.add(inv2s2 * ((fx * fx + fy * fy + fz * fz) - (gx * gx + gy * gy + gz * gz)));
       }
       if (sho) {
@@ -791,14 +788,9 @@ static __device__ __noinline__ double action_partial_mixed(const DevSys& s, cons
         acc.add(sa * dd + sb * rr);
       }
       if (prim && k < nlinks) {
-        double x = n1x, y = n1y, z = n1z;
-        pbc(s, x, y, z);
-        const float xn = (float)x, yn = (float)y, zn = (float)z;
-        x = o1x;
-        y = o1y;
-        z = o1z;
-        pbc(s, x, y, z);
-        const float xo = (float)x, yo = (float)y, zo = (float)z;
+        float xn, yn, zn, xo, yo, zo;
+        pbc_f(s, n1x, n1y, n1z, xn, yn, zn);
+        pbc_f(s, o1x, o1y, o1z, xo, yo, zo);
         const float r2n = xn * xn + yn * yn + zn * zn, r2o = xo * xo + yo * yo + zo * zo;
         acc.add((pa * (r2n - r2o) + pb * (r2n * r2n - r2o * r2o)) * ktau);
       }
@@ -829,12 +821,9 @@ static __device__ __noinline__ double action_partial_mixed(const DevSys& s, cons
         ax = m.s1x[t1 * np + ipart]; ay = m.s1y[t1 * np + ipart]; az = m.s1z[t1 * np + ipart];
         bx = m.s1x[t0 * np + ipart]; by = m.s1y[t0 * np + ipart]; bz = m.s1z[t0 * np + ipart];
       }
-      double dx = ax - pjx1, dy = ay - pjy1, dz = az - pjz1;
-      pbc(s, dx, dy, dz);
-      double px = bx - pjx0, py = by - pjy0, pz = bz - pjz0;
-      pbc(s, px, py, pz);
-      const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-      const float gx = (float)px, gy = (float)py, gz = (float)pz;
+      float fx, fy, fz, gx, gy, gz;
+      pbc_f(s, ax - pjx1, ay - pjy1, az - pjz1, fx, fy, fz);
+      pbc_f(s, bx - pjx0, by - pjy0, bz - pjz0, gx, gy, gz);
       const float r = sqrtf(fx * fx + fy * fy + fz * fz);
       const float rp = sqrtf(gx * gx + gy * gy + gz * gz);
       const float qq = 0.5f * (r + rp);
