@@ -76,6 +76,20 @@ typedef struct {
   double epsilon;
   int ewald;                           /* long-range Ewald term (needs an Ewald table) */
   int mover;                           /* PIMC_MOVER_* */
+  /* Sampler attributes of pi-qmc's <Sample> (src/parser/PIMCParser.cc:312-322),
+   * read by MultiLevelSampler / DoubleMLSampler.  Zero-initialised they are
+   * pi-qmc's defaults.  Every level's bisection width is
+   * sigma_factor sqrt(lambda tau 2^l) (defaultSigmaFactor; 0 means 1).  With
+   * delayed_rejection != 0, a level-(nlevel - 1) move that its uniform rejects
+   * gets a second proposal of width dr_sigma_factor sqrt(lambda tau 2^l)
+   * (newSigmaFactor; 0 means 0.75) and the delayed-rejection acceptance of
+   * src/advancer/MultiLevelSampler.cc:114-148 and
+   * src/advancer/DoubleMLSampler.cc:148-204.  Delayed rejection needs
+   * PIMC_MOVER_FREE (FreeMoverPBC leaves the forward probability of its first
+   * proposal unset). */
+  int delayed_rejection;
+  double sigma_factor;
+  double dr_sigma_factor;
 } pimc_system;
 
 /* A tabulated pair action, pi-qmc's PairAction::ugrid(ngpts,2,norder+1) on a

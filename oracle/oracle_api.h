@@ -47,6 +47,10 @@ typedef struct {
   int mover;                         /* 0 FreeMover, 1 FreeMoverPBC */
   uint64_t seed;
   uint32_t replica;
+  /* <Sample> attributes (src/parser/PIMCParser.cc:312-322); 0 = pi-qmc's defaults */
+  int delayed_rejection;             /* delayedRejection */
+  double sigma_factor;               /* defaultSigmaFactor (0 -> 1) */
+  double dr_sigma_factor;            /* newSigmaFactor (0 -> 0.75 with delayed rejection) */
 } ora_config;
 
 /* One attempted section move. */

@@ -33,6 +33,8 @@ class OraConfig(C.Structure):
         ("norder", C.c_int), ("ngpts", C.c_int), ("ewald", C.c_int),
         ("ewald_rcut", C.c_double), ("ewald_kcut", C.c_double), ("mover", C.c_int),
         ("seed", C.c_uint64), ("replica", C.c_uint32),
+        ("delayed_rejection", C.c_int), ("sigma_factor", C.c_double),
+        ("dr_sigma_factor", C.c_double),
     ]
 
 
@@ -108,6 +110,9 @@ def make_config(**kw):
     c.mover = kw.get("mover", 0)
     c.seed = kw.get("seed", 20261203)
     c.replica = kw.get("replica", 0)
+    c.delayed_rejection = int(kw.get("delayed_rejection", 0))
+    c.sigma_factor = kw.get("sigma_factor", 0.0)
+    c.dr_sigma_factor = kw.get("dr_sigma_factor", 0.0)
     return c
 
 
@@ -116,7 +121,7 @@ def build_port(force=False):
     src = os.path.join(HERE, "port.cc")
     if (not force and os.path.exists(PORT_LIB)
             and os.path.getmtime(PORT_LIB) >= max(
-                os.path.getmtime(src),
+                os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle_api.h")),
                 os.path.getmtime(os.path.join(REPO, "pi-qmc_gb300", "csrc", "pimc_rng.h")))):
         return PORT_LIB
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",

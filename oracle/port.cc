@@ -639,15 +639,18 @@ struct Sim {
   }
 
   // ---- Movers ----------------------------------------------------------
-  // FreeMover::makeMove (src/advancer/mover/FreeMover.cc:59-124).
-  double freeMove(int i, int level) {
+  // FreeMover::makeMove (src/advancer/mover/FreeMover.cc:59-124), at the
+  // sampler's current factor; forwardProb as getForwardProb() returns it.
+  double forwardProb = 0;
+  double freeMove(int i, int level, double factor) {
     const int nStride = 1 << level;
     const int ispec = spec[i];
     double toldOverTnew = 0;
+    forwardProb = 0;
     for (int islice = nStride; islice < nsec - nStride; islice += 2 * nStride) {
       double g[3];
       normals(g, 3);
-      double sigma = 1.0 * sqrt(lambda[i] * cfg.tau * nStride);
+      double sigma = factor * sqrt(lambda[i] * cfg.tau * nStride);
       double inv2Sigma2 = 0.5 / (sigma * sigma);
       double mid[3];
       for (int d = 0; d < 3; ++d) mid[d] = mov1[islice + nStride].x[d] - mov1[islice - nStride].x[d];
@@ -663,12 +666,16 @@ struct Sim {
       double temp = 1.0;
       for (int d = 0; d < 3; ++d) {
         const int pgi = (level * cfg.nspecies + ispec) * 3 + d;
-        if (has_pg_mover[pgi])
+        if (has_pg_mover[pgi]) {
           temp *= pg_mover[pgi].evaluate(delta[d]);
-        else
-          toldOverTnew += delta[d] * delta[d] * inv2Sigma2;
+        } else {
+          double tmp = delta[d] * delta[d] * inv2Sigma2;
+          forwardProb += tmp;
+          toldOverTnew += tmp;
+        }
       }
       temp = 1.0 / temp;
+      forwardProb += log(temp);
       for (int d = 0; d < 3; ++d)
         mid[d] = S1(islice + nStride, i).x[d] - S1(islice - nStride, i).x[d];
       cell.pbc(mid);
@@ -689,8 +696,60 @@ struct Sim {
     return toldOverTnew;
   }
 
+  // FreeMover::makeDelayedMove (src/advancer/mover/FreeMover.cc:127-185): the
+  // forward probability C->B of the rejected beads `rej` about the midpoints of
+  // the current moving beads (C), and the reverse B->C; returns ln(T_old/T_new)
+  // and leaves forwardProb.
+  double freeDelayedMove(int i, int level, double factor, const std::vector<V3>& rej) {
+    const int nStride = 1 << level;
+    const int ispec = spec[i];
+    double toldOverTnew = 0;
+    forwardProb = 0;
+    for (int islice = nStride; islice < nsec - nStride; islice += 2 * nStride) {
+      double sigma = factor * sqrt(lambda[i] * cfg.tau * nStride);
+      double inv2Sigma2 = 0.5 / (sigma * sigma);
+      double temp = 1.0;
+      double mid[3], delta[3];
+      for (int d = 0; d < 3; ++d) mid[d] = mov1[islice + nStride].x[d] - mov1[islice - nStride].x[d];
+      cell.pbc(mid);
+      for (int d = 0; d < 3; ++d) mid[d] *= 0.5;
+      for (int d = 0; d < 3; ++d) mid[d] += mov1[islice - nStride].x[d];
+      cell.pbc(mid);
+      for (int d = 0; d < 3; ++d) delta[d] = rej[islice].x[d] - mid[d];
+      cell.pbc(delta);
+      for (int d = 0; d < 3; ++d) {
+        const int pgi = (level * cfg.nspecies + ispec) * 3 + d;
+        if (has_pg_mover[pgi]) {
+          temp *= pg_mover[pgi].evaluate(delta[d]);
+        } else {
+          double tmp = delta[d] * delta[d] * inv2Sigma2;
+          forwardProb -= tmp;
+          toldOverTnew += tmp;
+        }
+      }
+      forwardProb += log(temp);
+      temp = 1.0 / temp;
+      for (int d = 0; d < 3; ++d) mid[d] = rej[islice + nStride].x[d] - rej[islice - nStride].x[d];
+      cell.pbc(mid);
+      for (int d = 0; d < 3; ++d) mid[d] *= 0.5;
+      for (int d = 0; d < 3; ++d) mid[d] += rej[islice - nStride].x[d];
+      cell.pbc(mid);
+      for (int d = 0; d < 3; ++d) delta[d] = mov1[islice].x[d] - mid[d];
+      cell.pbc(delta);
+      for (int d = 0; d < 3; ++d) {
+        const int pgi = (level * cfg.nspecies + ispec) * 3 + d;
+        if (has_pg_mover[pgi])
+          temp *= pg_mover[pgi].evaluate(delta[d]);
+        else
+          toldOverTnew -= delta[d] * delta[d] * inv2Sigma2;
+      }
+      toldOverTnew += log(temp);
+    }
+    return toldOverTnew;
+  }
+
   // FreeMoverPBC::makeMove (src/advancer/mover/FreeMoverPBC.cc:59-152).
-  double freeMovePBC(int i, int level) {
+  double freeMovePBC(int i, int level, double factor) {
     const int nStride = 1 << level;
     const int ispec = spec[i];
     double toldOverTnew = 0.;
@@ -701,7 +760,7 @@ struct Sim {
     for (int islice = nStride; islice < nsec - nStride; islice += 2 * nStride) {
       double g[3];
       normals(g, 3);
-      double sigma = 1.0 * sqrt(lambda[i] * cfg.tau * nStride);
+      double sigma = factor * sqrt(lambda[i] * cfg.tau * nStride);
       double inv2Sigma2 = 0.5 / (sigma * sigma);
       double mid[3], mid2[3];
       for (int d = 0; d < 3; ++d) mid[d] = mov1[islice + nStride].x[d] - mov1[islice - nStride].x[d];
@@ -859,24 +918,55 @@ struct Sim {
 
   // MultiLevelSampler::tryMove / DoubleMLSampler::tryMove
   // (src/advancer/MultiLevelSampler.cc:100-177, src/advancer/DoubleMLSampler.cc:123-245).
+  // With delayedRejection, level L - 1's rejected first proposal B gets a
+  // second proposal C (MultiLevelSampler.cc:114-148, DoubleMLSampler.cc:148-204);
+  // the records then hold C's values, as pi-qmc's last calls leave them.
   bool tryMove(int ipart, ora_record* rec) {
+    const double defaultFactor = cfg.sigma_factor != 0 ? cfg.sigma_factor : 1.0;
+    const double newFactor = cfg.dr_sigma_factor != 0 ? cfg.dr_sigma_factor : 0.75;
     double oldDeltaAction = 0;
-    for (int ilevel = L; ilevel >= 0; --ilevel) {
-      double lnTranProb = cfg.mover == 1 ? freeMovePBC(ipart, ilevel) : freeMove(ipart, ilevel);
-      double deltaAction = actionDiff(sec1, mov1, ipart, ilevel);
+    auto propose = [&](int ilevel, double factor, double& lnT, double& dS) {
+      lnT = cfg.mover == 1 ? freeMovePBC(ipart, ilevel, factor)
+                           : freeMove(ipart, ilevel, factor);
+      dS = actionDiff(sec1, mov1, ipart, ilevel);
       double dnode = 0;
       if (fixed_node)
         for (int sp = 0; sp < cfg.nspecies; ++sp)
           if (nodes[sp].kind) dnode += fnDiff(sp, ipart, ilevel);
       if (rec) {
-        rec->lnt[ilevel] = lnTranProb;
-        rec->ds[ilevel] = deltaAction;
+        rec->lnt[ilevel] = lnT;
+        rec->ds[ilevel] = dS;
         rec->ds_node[ilevel] = dnode;
       }
-      if (fixed_node) deltaAction += dnode;
+      if (fixed_node) dS += dnode;
+    };
+    for (int ilevel = L; ilevel >= 0; --ilevel) {
+      double lnTranProb, deltaAction;
+      propose(ilevel, defaultFactor, lnTranProb, deltaAction);
+      const double transA2B = forwardProb;
       double piRatioBoA = -deltaAction + oldDeltaAction;
       double acceptProb = exp(lnTranProb + piRatioBoA);
-      if (uniform() > acceptProb) {
+      if (cfg.delayed_rejection && ilevel == L - 1) {
+        if (uniform() > acceptProb) {
+          double accRatioA2B = acceptProb;
+          std::vector<V3> rej(mov1.begin(), mov1.end());
+          propose(ilevel, newFactor, lnTranProb, deltaAction);
+          double piRatioCoA = -deltaAction + oldDeltaAction;
+          double accRatioA2C = exp(lnTranProb + piRatioCoA);
+          lnTranProb = freeDelayedMove(ipart, ilevel, defaultFactor, rej);
+          double transC2B = forwardProb;
+          double accRatioC2B = exp(lnTranProb - piRatioCoA + piRatioBoA);
+          accRatioC2B = (accRatioC2B >= 1) ? 1 : accRatioC2B;
+          double accRatioA2B2C =
+              accRatioA2C * exp(transC2B + transA2B) * (1 - accRatioC2B) / (1 - accRatioA2B);
+          deltaAction = deltaAction - transC2B - transA2B -
+                        log((1 - accRatioC2B) / (1 - accRatioA2B));
+          if (uniform() > accRatioA2B2C) {
+            if (rec) rec->reject_level = ilevel;
+            return false;
+          }
+        }
+      } else if (uniform() > acceptProb) {
         if (rec) rec->reject_level = ilevel;
         return false;
       }

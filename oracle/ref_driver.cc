@@ -334,11 +334,17 @@ extern "C" void* ref_create(const ora_config* c) {
   s->mover = new RecMover(inner);
   s->chooser = 0;
   s->dchooser = 0;
+  // <Sample delayedRejection defaultSigmaFactor newSigmaFactor>, defaulted as
+  // PIMCParser does (src/parser/PIMCParser.cc:312-322)
+  const bool dr = c->delayed_rejection != 0;
+  const double defaultFactor = c->sigma_factor != 0 ? c->sigma_factor : 1.0;
+  const double newFactor = (dr && c->dr_sigma_factor == 0) ? 0.75 : c->dr_sigma_factor;
   if (!fixedNode) {
     s->chooser = new SectionChooser(c->nlevel, c->npart, *s->paths, *s->rec, bf);
     MultiLevelSampler* ml = new MultiLevelSampler(
         1, *s->paths, *s->chooser, new SimpleParticleChooser(c->npart, 1),
-        new PermutationChooser(1), *s->mover, s->rec, 1, bf, false, 1.0, 0.0, true);
+        new PermutationChooser(1), *s->mover, s->rec, 1, bf, dr, defaultFactor, newFactor,
+        true);
     s->chooser->resize(1);
     s->chooser->set(0, ml);
   } else {
@@ -347,7 +353,7 @@ extern "C" void* ref_create(const ora_config* c) {
     DoubleMLSampler* ml = new DoubleMLSampler(
         1, *s->paths, *s->dchooser, new SimpleParticleChooser(c->npart, 1),
         new PermutationChooser(1), new SimpleParticleChooser(c->npart, 1), 0, *s->mover,
-        s->rec, s->drec, false, 1, bf, false, 1.0, 0.0, true);
+        s->rec, s->drec, false, 1, bf, dr, defaultFactor, newFactor, true);
     s->dchooser->resize(1);
     s->dchooser->set(0, ml);
   }

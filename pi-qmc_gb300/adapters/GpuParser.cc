@@ -35,6 +35,9 @@ GpuActionSpec GpuParser::parseAction(const xmlNodePtr& gpu, const SimulationInfo
   const std::string seed = getStringAttribute(gpu, "seed");
   if (seed != "") spec.seed = std::stoull(seed);
   o.pbc_mover = getStringAttribute(gpu, "mover") != "Free";  // pi-qmc's default is FreePBC
+  spec.delayed_rejection = getBoolAttribute(gpu, "delayedRejection");
+  spec.sigma_factor = getDoubleAttribute(gpu, "defaultSigmaFactor");
+  spec.dr_sigma_factor = getDoubleAttribute(gpu, "newSigmaFactor");
   for (xmlNodePtr c = gpu->children; c; c = c->next) {
     if (c->type != XML_ELEMENT_NODE) continue;
     const std::string name = getName(c);
@@ -90,6 +93,9 @@ pimc_system GpuParser::system(const GpuActionSpec& spec, const SimulationInfo& s
     sys.prim_a[i] = spec.prim_a[i];
     sys.prim_b[i] = spec.prim_b[i];
   }
+  sys.delayed_rejection = spec.delayed_rejection ? 1 : 0;
+  sys.sigma_factor = spec.sigma_factor;
+  sys.dr_sigma_factor = spec.dr_sigma_factor;
   return sys;
 }
 
@@ -114,6 +120,9 @@ Algorithm* GpuParser::parseSample(const xmlNodePtr& node, Paths& paths, pimc_eng
   const std::string mover = getStringAttribute(node, "mover");
   if (mover != "" && (mover == "Free") == spec.opt.pbc_mover)
     throw std::runtime_error("GpuSample: mover differs from the GpuAction's");
+  if (getStringAttribute(node, "delayedRejection") != "" &&
+      getBoolAttribute(node, "delayedRejection") != spec.delayed_rejection)
+    throw std::runtime_error("GpuSample: delayedRejection differs from the GpuAction's");
   int attempts = getIntAttribute(node, "attempts");
   if (attempts <= 0) attempts = 1;
   return new GpuSectionSampler(paths, engine, attempts);

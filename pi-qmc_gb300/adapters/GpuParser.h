@@ -5,7 +5,8 @@
 // (INTEGRATION.md shows them):
 //
 //   <Action>                                   ActionParser::parse (src/parser/ActionParser.cc:105-153)
-//     <GpuAction nlevel="5" mover="FreePBC" precision="mixed" replicas="1" seed="20261203">
+//     <GpuAction nlevel="5" mover="FreePBC" precision="mixed" replicas="1" seed="20261203"
+//                delayedRejection="false" defaultSigmaFactor="1" newSigmaFactor="0.75">
 //       <SpringAction/>                        the usual pi-qmc action tags, with their
 //       <SHOAction omega="1" species="up"/>    own attribute names (ActionParser.cc:110-200,
 //       <PrimSHOAction a="0.5" b="0.1"/>       307-320, 433-452, 760-790); a tag without
@@ -17,8 +18,11 @@
 //
 // Numbers are read in the simulation's internal units (Hartree, bohr); unit
 // suffixes are not converted.  Node models: SHONodes and FreeParticleNodes.
-// The bisection mover is part of the engine, so it is named on <GpuAction>
-// (`mover`, "Free" or "FreePBC", pi-qmc's default) rather than on the sampler.
+// The bisection mover and the sampler's width factors and delayed rejection
+// are part of the engine, so they are named on <GpuAction> (`mover`, "Free" or
+// "FreePBC", pi-qmc's default; `delayedRejection`, `defaultSigmaFactor`,
+// `newSigmaFactor`, pi-qmc's <Sample> attribute names) rather than on the
+// sampler; a <GpuSample> that repeats one of them must agree.
 #ifndef PIMC_GB300_GPU_PARSER_H
 #define PIMC_GB300_GPU_PARSER_H
 
@@ -37,6 +41,10 @@ struct GpuActionSpec {
   int norder = 3;                      // CoulombAction norder
   double ewald_rcut = 0, ewald_kcut = 0;
   int precision = PIMC_PREC_FP64;
+  // the bisection sampler's <Sample> attributes (src/parser/PIMCParser.cc:312-322):
+  // delayedRejection, defaultSigmaFactor, newSigmaFactor (0: pi-qmc's defaults)
+  bool delayed_rejection = false;
+  double sigma_factor = 0, dr_sigma_factor = 0;
   int replicas = 1;
   unsigned long long seed = 20261203ull;
 };
@@ -53,8 +61,8 @@ class GpuParser : public XMLParser {
   // makes (pimc_coulomb_tables reproduces CoulombAction's to 7e-15 relative).
   static pimc_engine* createEngine(const GpuActionSpec& spec, const SimulationInfo& simInfo);
   // <GpuSample attempts=.. mover="Free|FreePBC">: the device sampler.  The
-  // mover is fixed when the engine is built, so a `mover` that disagrees with
-  // the GpuAction's throws.
+  // mover and the sampler attributes are fixed when the engine is built, so a
+  // `mover` or `delayedRejection` that disagrees with the GpuAction's throws.
   static Algorithm* parseSample(const xmlNodePtr& gpuSample, Paths& paths, pimc_engine* engine,
                                 const GpuActionSpec& spec);
 

@@ -219,6 +219,11 @@ int validate(const pimc_system& s) {
   if (s.nlevel < 1 || s.nlevel > PIMC_MAX_LEVEL)
     return fail(PIMC_ERR_CAPACITY, "nlevel must be in 1..6");
   if (!(s.tau > 0)) return fail(PIMC_ERR_INVALID, "tau must be positive");
+  if (!(s.sigma_factor >= 0) || !(s.dr_sigma_factor >= 0) || !std::isfinite(s.sigma_factor) ||
+      !std::isfinite(s.dr_sigma_factor))
+    return fail(PIMC_ERR_INVALID, "sigma factors must be finite and non-negative");
+  if (s.delayed_rejection && s.mover != PIMC_MOVER_FREE)
+    return fail(PIMC_ERR_INVALID, "delayed rejection needs the FreeMover");
   bool fixed = false;
   for (int i = 0; i < s.nspecies; ++i) fixed |= s.node_kind[i] != 0;
   // A section of 2^nlevel + 1 slices may span the whole ring (nslice = 2^nlevel,
@@ -290,9 +295,19 @@ void fill_sys(const pimc_system& s, DevSys& d) {
     for (int i = 0; i < s.nspecies; ++i) {
       const double lam = 0.5 / s.spec_mass[i];
       d.spr_inv2s2[lev][i] = 0.25 / (lam * s.tau * nStride);
-      const double sigma = 1.0 * std::sqrt(lam * s.tau * nStride);
+      // FreeMover: sigma = factor sqrt(lambda tau 2^l), factor = defaultSigmaFactor
+      // (0 means 1, src/parser/PIMCParser.cc:316-319)
+      const double factor = s.sigma_factor != 0 ? s.sigma_factor : 1.0;
+      const double sigma = factor * std::sqrt(lam * s.tau * nStride);
       d.mov_sigma[lev][i] = sigma;
       d.mov_inv2s2[lev][i] = 0.5 / (sigma * sigma);
+      if (s.delayed_rejection && lev == s.nlevel - 1) {
+        // the second proposal: newSigmaFactor (0 means 0.75, PIMCParser.cc:320-322)
+        const double nf = s.dr_sigma_factor != 0 ? s.dr_sigma_factor : 0.75;
+        const double sg = nf * std::sqrt(lam * s.tau * nStride);
+        d.dr_sigma[i] = sg;
+        d.dr_inv2s2[i] = 0.5 / (sg * sg);
+      }
       if (s.sho_omega[i] > 0) {
         const double wt = s.sho_omega[i] * s.tau * nStride;
         d.sho_cosh[lev][i] = std::cosh(wt);
@@ -331,6 +346,7 @@ void fill_sys(const pimc_system& s, DevSys& d) {
   d.coulomb = s.coulomb;
   d.ewald = s.ewald;
   d.mover = s.mover;
+  d.dr = s.delayed_rejection != 0;
   d.epsilon = s.epsilon > 0 ? s.epsilon : 1.0;
 }
 

@@ -193,7 +193,9 @@ static __device__ __noinline__ void store_section(const DevSys& s, double* path,
 // form's on identical moves.
 static __device__ __noinline__ void attempt_normals(const DevSys& s, const Smem& m, uint64_t seed,
                                        uint32_t rep, uint32_t att) {
-  const int nord = (1 << s.nlevel) - 1;
+  // (with delayed rejection one more: the second proposal at level nlevel - 1
+  // takes order 1, the slices after it one order later)
+  const int nord = (1 << s.nlevel) - 1 + (s.dr ? 1 : 0);
   for (int o = threadIdx.x; o < nord; o += blockDim.x) {
     double z0, z1, z2, z3;
     stream_normal_pair(seed, rep, att, 2u * o, &z0, &z1);
@@ -204,15 +206,18 @@ static __device__ __noinline__ void attempt_normals(const DevSys& s, const Smem&
   }
 }
 
+// oshift: moved-slice orders taken by a delayed-rejection proposal before
+// this level; second: the delayed-rejection proposal itself (its width).
 static __device__ __noinline__ double mover_level_part(const DevSys& s, const Smem& m, int ipart, int level,
-                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
+                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase,
+                              int oshift = 0, bool second = false) {
   const int L = s.nlevel, np = s.npart;
   const int nStride = 1 << level;
   const int nmov = (level == L) ? 0 : (1 << (L - level - 1));
-  const int ord0 = (level == L) ? 0 : (1 << (L - level - 1)) - 1;
+  const int ord0 = ((level == L) ? 0 : (1 << (L - level - 1)) - 1) + oshift;
   const int sp = species_of(s, ipart);
-  const double sigma = s.mov_sigma[level][sp];
-  const double inv2Sigma2 = s.mov_inv2s2[level][sp];
+  const double sigma = second ? s.dr_sigma[sp] : s.mov_sigma[level][sp];
+  const double inv2Sigma2 = second ? s.dr_inv2s2[sp] : s.mov_inv2s2[level][sp];
   double part = 0.0;
   for (int k = threadIdx.x; k < nmov; k += blockDim.x) {
     const int t = nStride * (2 * k + 1), tp = t - nStride, tn = t + nStride;
@@ -295,9 +300,12 @@ static __device__ __noinline__ double mover_level_part(const DevSys& s, const Sm
 
 // FreeMover(PBC)::makeMove for one level: the beads, and ln(T_old/T_new) summed over the block.
 static __device__ double mover_level(const DevSys& s, const Smem& m, int ipart, int level,
-                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase) {
-  return block_sum(mover_level_part(s, m, ipart, level, seed, rep, att, ubase), m.red);
+                              uint64_t seed, uint32_t rep, uint32_t att, uint32_t ubase,
+                              int oshift = 0, bool second = false) {
+  return block_sum(mover_level_part(s, m, ipart, level, seed, rep, att, ubase, oshift, second),
+                   m.red);
 }
+
 
 // Block sums of nv per-thread values (nv <= 8) in a fixed order: warp trees,
 // then the warps in turn; out[v] is visible to every thread on return.
@@ -786,6 +794,98 @@ static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, d
 }
 
 
+// MultiLevelSampler::tryMove's delayed rejection (src/advancer/MultiLevelSampler.cc:114-148;
+// DoubleMLSampler.cc:148-204 with the node term) after the first proposal B at
+// level L - 1 was rejected: the second proposal C (width newSigmaFactor, the
+// next normals), its action difference, FreeMover::makeDelayedMove
+// (src/advancer/mover/FreeMover.cc:127-185) for the forward C->B and reverse
+// B->C probabilities, and the combined acceptance with the next uniform.
+// Thread 0 holds piRatioBoA and the acceptance of B in red[kWarps + 3, 4];
+// returns the level-(L - 1) rejection (C_REJECT) and, when C is accepted, the
+// modified action difference in red[kWarps + 2].
+static __device__ __noinline__ void delayed_rejection(const DevSys& s, const Smem& m, double scale,
+                                                     int msp, int ipart, bool mynode,
+                                                     double* cache, int ifirst1, int ep,
+                                                     uint64_t seed, uint32_t att, uint32_t uacc,
+                                                     double oldDS, long long* ek,
+                                                     long long* ekstage, pimc_move_record* rec,
+                                                     uint32_t* status) {
+  const int L = s.nlevel, level = L - 1, nsec = s.nsec;
+  const int t = 1 << level, tp = 0, tn = nsec - 1;
+  const int sp = species_of(s, ipart);
+  double* bead = m.red + kWarps + 5;  // the rejected bead B
+  if (threadIdx.x == 0) {
+    bead[0] = m.mx[t];
+    bead[1] = m.my[t];
+    bead[2] = m.mz[t];
+  }
+  __syncthreads();
+  // C: FreeMover::makeMove with factor = newFactor and the next normals
+  const double lnTC = mover_level(s, m, ipart, level, seed, s.stream_id, att, uacc, 1, true);
+  double dsC = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
+  if (s.ewald && s.coulomb && level == 0) {
+    if (ek)
+      dsC += ewald_level0_cached(s, m, ipart, ifirst1, ek, ekstage);
+    else
+      for (int k = 1; k < nsec - 1; ++k) dsC += ewald_slice_diff(s, m, ipart, k);
+  }
+  double dsnC = 0.0;
+  if (mynode) dsnC = node_level(s, m, scale, msp, ipart, level, cache, ifirst1, ep);
+  if (threadIdx.x == 0) {
+    const double piRatioBoA = m.red[kWarps + 3], accRatioA2B = m.red[kWarps + 4];
+    const double sigma = s.mov_sigma[level][sp], inv2Sigma2 = s.mov_inv2s2[level][sp];
+    // transA2B = B's forward probability: its Gaussian step, as makeMove drew it
+    double dx = m.nrm[0] * sigma, dy = m.nrm[1] * sigma, dz = m.nrm[2] * sigma;
+    pbc(s, dx, dy, dz);
+    double transA2B = 0.0;
+    transA2B += dx * dx * inv2Sigma2;
+    transA2B += dy * dy * inv2Sigma2;
+    transA2B += dz * dz * inv2Sigma2;
+    transA2B += log(1.0);
+    const double deltaC = s.fixed_node ? dsC + dsnC : dsC;
+    const double piRatioCoA = -deltaC + oldDS;
+    const double accRatioA2C = exp(lnTC + piRatioCoA);
+    // makeDelayedMove with factor = defaultFactor: the midpoint of the level's
+    // neighbours (the section ends, the same for B and C), B and C about it
+    double mx = m.mx[tn] - m.mx[tp], my = m.my[tn] - m.my[tp], mz = m.mz[tn] - m.mz[tp];
+    pbc(s, mx, my, mz);
+    mx *= 0.5; my *= 0.5; mz *= 0.5;
+    mx += m.mx[tp]; my += m.my[tp]; mz += m.mz[tp];
+    pbc(s, mx, my, mz);
+    double bx = bead[0] - mx, by = bead[1] - my, bz = bead[2] - mz;
+    pbc(s, bx, by, bz);
+    double forwardProb = 0.0, toldOverTnew = 0.0, tmp;
+    tmp = bx * bx * inv2Sigma2; forwardProb -= tmp; toldOverTnew += tmp;
+    tmp = by * by * inv2Sigma2; forwardProb -= tmp; toldOverTnew += tmp;
+    tmp = bz * bz * inv2Sigma2; forwardProb -= tmp; toldOverTnew += tmp;
+    forwardProb += log(1.0);
+    double cx = m.mx[t] - mx, cy = m.my[t] - my, cz = m.mz[t] - mz;
+    pbc(s, cx, cy, cz);
+    toldOverTnew -= cx * cx * inv2Sigma2;
+    toldOverTnew -= cy * cy * inv2Sigma2;
+    toldOverTnew -= cz * cz * inv2Sigma2;
+    toldOverTnew += log(1.0);
+    const double transC2B = forwardProb;
+    double accRatioC2B = exp(toldOverTnew - piRatioCoA + piRatioBoA);
+    accRatioC2B = (accRatioC2B >= 1) ? 1 : accRatioC2B;
+    const double accRatioA2B2C = accRatioA2C * exp(transC2B + transA2B) * (1 - accRatioC2B) /
+                                 (1 - accRatioA2B);
+    const double delta =
+        deltaC - transC2B - transA2B - log((1 - accRatioC2B) / (1 - accRatioA2B));
+    if (rec) {
+      rec->ds[level] = dsC;
+      rec->ds_node[level] = dsnC;
+      rec->lnt[level] = lnTC;
+    }
+    if (!(isfinite(lnTC) && isfinite(dsC))) *status |= PIMC_STATUS_NONFINITE;
+    const double u = stream_uniform(seed, s.stream_id, att, uacc + 1u);
+    m.ictl[C_REJECT] = (u > accRatioA2B2C) ? level : -1;
+    m.red[kWarps + 2] = delta;
+  }
+  __syncthreads();
+}
+
+
 // NT (largest block) and MINB set the register budget, 65536 / (NT * MINB)
 // per thread; the variants are compiled in separate translation units
 // (section_variants.cu) and chosen at run time by the launch configuration.
@@ -887,7 +987,9 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       // their Slater matrices side by side; the decisions then follow level by
       // level exactly as below.  Work done for levels under a rejection is
       // discarded.
-      const int lb = L >= 2 ? max(1, L - 3) : L + 1;
+      // (with delayed rejection every level is taken in turn: a second proposal
+      // at level L - 1 changes the normals and uniforms of the levels under it)
+      const int lb = (L >= 2 && !s.dr) ? max(1, L - 3) : L + 1;
       if (lb <= L) {
         double* lds = m.red + kWarps + 8;  // [kMaxLevels] per level: action difference,
         double* llt = lds + kMaxLevels;     // mover ln T,
@@ -938,9 +1040,11 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         reject = m.ictl[C_REJECT];
         oldDS = m.red[kWarps + 2];
       }
+      int oshift = 0;   // moved-slice orders and uniforms a delayed-rejection
+      uint32_t ushift = 0;  // proposal took before the level
       for (int level = min(L, lb - 1); level >= 0 && reject < 0; --level) {
-        const uint32_t ubase = level_uniform_base(s, level);
-        const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase);
+        const uint32_t ubase = level_uniform_base(s, level) + ushift;
+        const double lnT = mover_level(s, m, ipart, level, P.seed, s.stream_id, att, ubase, oshift);
         double ds = block_sum(action_partial(s, m, ipart, level, threadIdx.x, blockDim.x), m.red);
         if (s.ewald && s.coulomb && level == 0) {
           if (ek)
@@ -965,9 +1069,20 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
           if (!(isfinite(lnT) && isfinite(ds))) status |= PIMC_STATUS_NONFINITE;
           if (u > p) m.ictl[C_REJECT] = level;
           m.red[kWarps + 2] = total;
+          m.red[kWarps + 3] = -total + oldDS;  // piRatioBoA
+          m.red[kWarps + 4] = p;               // accRatioA2B
         }
         __syncthreads();
         reject = m.ictl[C_REJECT];
+        if (reject == L - 1 && s.dr) {
+          const uint32_t nmov = 1u << (L - level - 1);
+          const uint32_t uacc = ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
+          delayed_rejection(s, m, scale[msp], msp, ipart, mynode, cache, ifirst1, epoch[msp],
+                            P.seed, att, uacc, oldDS, ek, ekstage, rec, &status);
+          reject = m.ictl[C_REJECT];
+          oshift = 1;
+          ushift = 1;
+        }
         if (reject >= 0) break;
         oldDS = m.red[kWarps + 2];
       }

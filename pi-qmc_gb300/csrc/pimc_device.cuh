@@ -47,6 +47,10 @@ struct DevSys {
   // The mixed form's SHO link action without cancellation:
   // a |r1 - r0|^2 + b r0.r1, a = (m / 2 tau') (x coth x - 1), b = m w tanh(x / 2), x = w tau'
   float sho_a[kMaxLevels][kMaxSpecies], sho_b[kMaxLevels][kMaxSpecies];
+  // Delayed rejection (MultiLevelSampler's delayedRejection): on, and the
+  // second proposal's width and 1 / (2 width^2) at level nlevel - 1
+  int dr;
+  double dr_sigma[kMaxSpecies], dr_inv2s2[kMaxSpecies];
   double cell[3], cellb[3], rcut2;
   float rcut2_lo;  // the mixed form's FP32 pre-test of pbc (pbc_f): rcut2 (1 - 1e-5)
   int spring, coulomb, ewald, mover, fixed_node;

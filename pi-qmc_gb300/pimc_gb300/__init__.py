@@ -40,6 +40,8 @@ class System(C.Structure):
         ("node_temperature", C.c_double), ("nslice", C.c_int), ("tau", C.c_double),
         ("nlevel", C.c_int), ("cell", C.c_double * 3), ("spring", C.c_int),
         ("coulomb", C.c_int), ("epsilon", C.c_double), ("ewald", C.c_int), ("mover", C.c_int),
+        ("delayed_rejection", C.c_int), ("sigma_factor", C.c_double),
+        ("dr_sigma_factor", C.c_double),
     ]
 
 
@@ -128,6 +130,10 @@ def system_from_kw(kw):
     s.epsilon = kw.get("epsilon", 1.0)
     s.ewald = kw.get("ewald", 0)
     s.mover = kw.get("mover", 0)
+    # <Sample delayedRejection defaultSigmaFactor newSigmaFactor> (0: pi-qmc's defaults)
+    s.delayed_rejection = int(kw.get("delayed_rejection", 0))
+    s.sigma_factor = kw.get("sigma_factor", 0.0)
+    s.dr_sigma_factor = kw.get("dr_sigma_factor", 0.0)
     return s
 
 

@@ -55,7 +55,8 @@ int main() {
   static const char* const pa[] = {"species", "dn", "a", "0.5", "b", "0.25", 0};
   static const char* const sa[] = {"omega", "1", 0};
   static const char* const ga[] = {"nlevel", "3", "mover", "Free", "precision", "mixed",
-                                   "replicas", "7", 0};
+                                   "replicas", "7", "delayedRejection", "true",
+                                   "newSigmaFactor", "0.6", 0};
   static const char* const none[] = {0};
   xmlNode fn_dn = elem("FixedNodeAction", fna);
   xmlNode fn_up = elem("FixedNodeAction", fua, 0, &fn_dn);
@@ -74,6 +75,7 @@ int main() {
          s.nslice, s.tau, s.nlevel, s.epsilon, s.spring, s.coulomb, (double)spec.norder, s.mover,
          spec.replicas);
   printf("%d\n", spec.precision);
+  printf("%d %g %g\n", s.delayed_rejection, s.sigma_factor, s.dr_sigma_factor);
 
   // an unknown child and a mover that disagrees are refused
   xmlNode bad = elem("EwaldAction", none);
@@ -91,7 +93,14 @@ int main() {
   } catch (const std::runtime_error&) {
     refused += 1;
   }
-  static const char* const smb[] = {"attempts", "640", 0};
+  static const char* const smd[] = {"attempts", "640", "delayedRejection", "false", 0};
+  xmlNode smpd = elem("GpuSample", smd);
+  try {
+    pimc_gb300::GpuParser::parseSample(&smpd, *(Paths*)ref_paths(h), 0, spec);
+  } catch (const std::runtime_error&) {
+    refused += 1;
+  }
+  static const char* const smb[] = {"attempts", "640", "delayedRejection", "true", 0};
   xmlNode smp2 = elem("GpuSample", smb);
   Algorithm* a = pimc_gb300::GpuParser::parseSample(&smp2, *(Paths*)ref_paths(h), 0, spec);
   printf("%d %d\n", refused, a != 0);

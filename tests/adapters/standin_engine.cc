@@ -77,6 +77,9 @@ int pimc_engine_create(const pimc_system* sys, int nreplica, const pimc_pair_tab
   c.norder = ntables > 0 ? tables[0].norder : 3;
   c.ewald = sys->ewald;
   c.mover = sys->mover;
+  c.delayed_rejection = sys->delayed_rejection;
+  c.sigma_factor = sys->sigma_factor;
+  c.dr_sigma_factor = sys->dr_sigma_factor;
   c.seed = seed;
   c.replica = 0;
   std::vector<int> species(2 * (ntables > 0 ? ntables : 1));

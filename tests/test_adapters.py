@@ -182,12 +182,14 @@ def test_gpu_tags_parse_into_the_engine_system(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
     lines = [l for l in out.stdout.splitlines() if l and l[0].isdigit()]
-    v = lines[-3].split()
+    v = lines[-4].split()
     # npart nspecies counts sho_omega prim_a prim_a prim_b mass charge cell node_kind
     # node_omega node_temperature nslice tau nlevel epsilon spring coulomb norder mover replicas
     assert v[:12] == ["4", "2", "2", "2", "1", "1", "0", "0.5", "0.25", "1", "-1", "1000"]
     assert v[12:17] == ["1", "1", "1.25", "1.5", "0.5"]
     assert v[17] == "64" and float(v[18]) == 4.0 / 64 and v[19] == "3"
     assert v[20:26] == ["2", "1", "1", "3", "0", "7"]
-    assert lines[-2] == "1"              # precision: mixed
-    assert lines[-1] == "2 1"            # both refusals, and a sampler
+    assert lines[-3] == "1"              # precision: mixed
+    # delayedRejection, defaultSigmaFactor (0: pi-qmc's default), newSigmaFactor
+    assert lines[-2] == "1 0 0.6"
+    assert lines[-1] == "3 1"            # the three refusals, and a sampler

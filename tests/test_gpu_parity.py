@@ -347,7 +347,7 @@ def test_graph_steps_equal_direct_calls(pimc):
     assert a.kernel_launches - n0 == 9
 
 
-@pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small"])
+@pytest.mark.parametrize("case", ["dot4_fn", "heg8", "dot2_small", "dot4_dr"])
 @pytest.mark.parametrize("block,scratch_global,regs", [(64, 0, 4), (128, 1, 3), (256, 1, 2),
                                                        (256, 2, 3), (128, 2, 2),
                                                        (256, 0, 3), (512, 1, 1), (512, 0, 1)])
@@ -470,7 +470,8 @@ def test_displace_matches_golden(pimc, case):
     assert np.abs(e.download_paths()[0] - d["path"]).max() <= 1e-12
 
 
-@pytest.mark.parametrize("case", ["dot4_fn", "dot2_full", "heg8", "heg16_hot", "dot20_fn"])
+@pytest.mark.parametrize("case", ["dot4_fn", "dot2_full", "heg8", "heg16_hot", "dot20_fn",
+                                  "dot2_dr", "dot4_dr"])
 def test_mixed_form_on_identical_proposals(pimc, case):
     # Both precision forms draw the same FP64 proposals, so a mixed chain follows
     # the FP64 chain until a uniform falls within the mixed error of its

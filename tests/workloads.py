@@ -27,6 +27,13 @@ GOLDEN_CASES = {
     # SHOAction omega = 0.5, kT = 1, M = 32, level 5 (a section spans the ring)
     "sho_system": (dot2(counts=[1], sho_omega=[0.5], nslice=32, beta=1.0, nlevel=5, coulomb=0,
                         cell=20.0), "gauss", 600),
+    # delayed rejection (<Sample delayedRejection="true">): MultiLevelSampler on
+    # the plain dot with defaultSigmaFactor 1.3 and newSigmaFactor 0.6, and
+    # DoubleMLSampler on the small fixed-node dot with pi-qmc's defaults (1, 0.75)
+    "dot2_dr": (dot2(nslice=64, delayed_rejection=1, sigma_factor=1.3, dr_sigma_factor=0.6),
+                "gauss", 600),
+    "dot4_dr": (dot20_fn(counts=[2, 2], nslice=64, beta=4.0, nlevel=3, delayed_rejection=1),
+                "const", 400),
 }
 
 # NodeModel fixtures (tests/golden/nodes_<case>.npz): pi-qmc's own
