@@ -163,7 +163,9 @@ int pimc_set_stream(pimc_engine* e, void* stream);
 
 /* ---- paths (SerialPaths::getBeads/putBeads, src/base/SerialPaths.cc:119-185) */
 
-/* Host <-> device copies of all replicas' paths (host layout above). */
+/* Host <-> device copies of all replicas' paths (host layout above).  An
+ * upload rebuilds the cached per-slice results (Slater entries, structure
+ * factors) of the slices whose beads changed, bit for bit as a full rebuild. */
 int pimc_upload_paths(pimc_engine* e, const double* host_xyz);
 int pimc_download_paths(pimc_engine* e, double* host_xyz);
 /* Offsets (in doubles) of each replica's path in the packed host layout; for

@@ -89,6 +89,7 @@ struct DevBuf {
     if (count == 0) return 0;
     if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
       p = nullptr;
+      n = 0;
       return -1;
     }
     return 0;
@@ -126,6 +127,8 @@ struct pimc_engine {
   DevBuf<long long> d_ekcache;  // structure factors per replica and slice
   DevBuf<long long> d_ekstage;  // per-CTA staging of an attempt's new structure factors
   int ekstage_stride = 0;       // int64 words per CTA
+  DevBuf<double> d_upload;      // pimc_upload_paths: the host paths, before comparison
+  DevBuf<unsigned char> d_changed;  // [replica][nslice_max]: slices the upload changed
   DevBuf<double> d_xstage;      // mixed form: per-CTA staging of changed slices' inverses
   long long xstage_cta = 0;     // doubles per CTA
   DevBuf<int> d_order;
@@ -181,6 +184,8 @@ struct pimc_engine {
     d_prefill_scr.free();
     d_ekstage.free();
     d_xstage.free();
+    d_upload.free();
+    d_changed.free();
     d_order.free();
     d_next.free();
     d_pool.free();
@@ -562,7 +567,8 @@ int device_check(int& nsm) {
   return 0;
 }
 
-int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot);
+int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot,
+                  const unsigned char* changed = nullptr);
 
 int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables,
                  const int* tab_off, int uniform, const pimc_ewald_table* ewald, uint64_t seed,
@@ -852,7 +858,8 @@ int pimc_set_stream(pimc_engine* e, void* stream) {
 namespace {
 // Fills the Slater-result cache entries of `nslot` replicas (slots on the device,
 // or null for 0 .. nslot-1) from their current paths, one warp per entry.
-int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) {
+int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot,
+                  bool only_invalid = false) {
   int nsp = 0, mmax = 0, nmax = 0;
   bool anyfree = false, any = false;
   for (int r = 0; r < e->nrep; ++r) {
@@ -875,6 +882,7 @@ int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) 
   P.cache = cache;
   P.slots = d_slots;
   P.nslot = nslot;
+  P.only_invalid = only_invalid ? 1 : 0;
   P.ntask_per_slot = nsp * mmax;
   P.stage_stride = (6 * nmax + 1) & ~1;
   // Slater scratch: all of it in shared memory up to 6 KB a warp; else its hot
@@ -915,7 +923,7 @@ int prefill_cache(pimc_engine* e, double* cache, const int* d_slots, int nslot) 
 
 // Fills the structure-factor cache of `nslot` replicas (device slot list, or
 // null for 0 .. nslot-1) from their current paths.
-int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot) {
+int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot, const unsigned char* changed) {
   if (!e->d_ekcache.p || nslot == 0) return PIMC_OK;
   int mmax = 0, np = 0, per = 0;
   for (const DevSys& d : e->hsys) {
@@ -932,6 +940,7 @@ int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot) {
   P.slots = d_slots;
   P.nslot = nslot;
   P.nslice_max = mmax;
+  P.changed = changed;
   const size_t smem = (size_t)per * np * 16 + (size_t)np * 8;
   if (smem > 200 * 1024) return fail(PIMC_ERR_CAPACITY, "Ewald tables exceed shared memory");
   cudaFuncSetAttribute(ewald_prefill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -945,11 +954,34 @@ int prefill_ewald(pimc_engine* e, const int* d_slots, int nslot) {
 
 extern "C" {
 
+// The upload lands in a staging buffer; a kernel compares it with the
+// engine's paths slice by slice, copies the slices that differ and flags
+// them, and only the cached results that depend on a changed slice (Slater
+// entries pairing it, its structure factors) are rebuilt.  The caches are
+// consistent with the engine's paths after every call (moves keep them so),
+// so the rebuilt and kept entries together equal a full rebuild bit for bit.
 int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (!e || !host_xyz) return fail(PIMC_ERR_INVALID, "null argument");
   if (e->server) return fail(PIMC_ERR_INVALID, "a server takes paths at admission");
-  CU(cudaMemcpyAsync(e->d_paths.p, host_xyz, e->path_off[e->nrep] * sizeof(double),
-                     cudaMemcpyHostToDevice, e->stream));
+  const size_t n = e->path_off[e->nrep];
+  int mmax = 1;
+  for (const DevSys& d : e->hsys) mmax = std::max(mmax, d.nslice);
+  const size_t nflag = (size_t)e->nrep * mmax;
+  if (e->d_upload.n < n || e->d_changed.n < nflag) {
+    CU(cudaStreamSynchronize(e->stream));
+    if ((e->d_upload.n < n && e->d_upload.alloc(n)) ||
+        (e->d_changed.n < nflag && e->d_changed.alloc(nflag)))
+      return fail(PIMC_ERR_CUDA, "cudaMalloc upload staging");
+  }
+  CU(cudaMemcpyAsync(e->d_upload.p, host_xyz, n * sizeof(double), cudaMemcpyHostToDevice,
+                     e->stream));
+  {
+    const dim3 grid((unsigned)mmax, (unsigned)std::min(e->nrep, 65535));
+    path_update_kernel<<<grid, 128, 0, e->stream>>>(e->d_sys.p, e->d_paths.p, e->d_upload.p,
+                                                    e->d_changed.p, mmax, e->nrep);
+    CU(cudaGetLastError());
+    e->launches++;
+  }
   {
     const dim3 grid(16, (unsigned)std::min(e->nrep, 65535));
     path_scan_kernel<<<grid, kBlock, 0, e->stream>>>(e->d_sys.p, e->d_state.p, e->d_paths.p,
@@ -957,11 +989,15 @@ int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
     CU(cudaGetLastError());
     e->launches++;
   }
-  if (e->d_nodecache.p) {  // new paths: every cached Slater result is rebuilt
-    CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double), e->stream));
-    if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep)) return rc;
+  if (e->d_nodecache.p) {
+    const dim3 grid(8, (unsigned)std::min(e->nrep, 65535));
+    cache_invalidate_kernel<<<grid, 128, 0, e->stream>>>(e->d_sys.p, e->d_nodecache.p,
+                                                         e->d_changed.p, mmax, e->nrep);
+    CU(cudaGetLastError());
+    e->launches++;
+    if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep, true)) return rc;
   }
-  return prefill_ewald(e, nullptr, e->nrep);
+  return prefill_ewald(e, nullptr, e->nrep, e->d_changed.p);
 }
 
 int pimc_download_paths(pimc_engine* e, double* host_xyz) {

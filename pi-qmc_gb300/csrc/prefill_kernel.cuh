@@ -31,6 +31,51 @@ __global__ void __launch_bounds__(kBlock) path_scan_kernel(const DevSys* sys, De
   }
 }
 
+// An upload of paths over the engine's current ones (pimc_upload_paths):
+// block (t, r) compares slice t of replica r bit for bit, copies it when it
+// differs and flags it in changed[r][t] (nslice_max per replica).
+__global__ void __launch_bounds__(kBlock) path_update_kernel(const DevSys* sys, double* paths,
+                                                             const double* upload,
+                                                             unsigned char* changed,
+                                                             int nslice_max, int nrep) {
+  const int t = blockIdx.x;
+  for (int r = blockIdx.y; r < nrep; r += gridDim.y) {  // block-uniform
+    const DevSys& s = sys[r];
+    if (t >= s.nslice) continue;
+    const int n = 3 * s.npart;
+    const size_t o = s.path_offset + (size_t)t * n;
+    const long long* a = (const long long*)(paths + o);
+    const long long* b = (const long long*)(upload + o);
+    int diff = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) diff |= a[i] != b[i];
+    diff = __syncthreads_or(diff);
+    if (diff)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) paths[o + i] = upload[o + i];
+    if (threadIdx.x == 0) changed[(size_t)r * nslice_max + t] = diff ? 1 : 0;
+  }
+}
+
+// The Slater-result entries that pair a changed slice (as r1 on slice t or as
+// r2 on slice t - M/2) are invalidated: entry (r, species, t) for a changed t
+// or t + M/2.
+__global__ void cache_invalidate_kernel(const DevSys* sys, double* cache,
+                                        const unsigned char* changed, int nslice_max, int nrep) {
+  const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+  for (int r = blockIdx.y; r < nrep; r += gridDim.y) {
+    const DevSys& s = sys[r];
+    if (!s.fixed_node || s.nc_offset < 0) continue;
+    const int M = s.nslice;
+    const unsigned char* c = changed + (size_t)r * nslice_max;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < s.nspecies * M;
+         it += gridDim.x * blockDim.x) {
+      const int sp = it / M, t = it - sp * M;
+      if (!s.node_kind[sp]) continue;
+      if (c[t] || c[(t + M / 2) % M])
+        cache[s.nc_offset + ((size_t)sp * M + t) * s.nc_stride] = NaN;
+    }
+  }
+}
+
 struct PrefillParams {
   const DevSys* sys;
   const DevState* state;
@@ -38,6 +83,7 @@ struct PrefillParams {
   double* cache;       // the cache pool (entries at sys.nc_offset)
   const int* slots;    // replicas to fill (null: 0 .. nslot-1)
   int nslot;
+  int only_invalid;    // skip the entries that are valid (of the current scale)
   int ntask_per_slot;  // nspecies_max x nslice_max
   int stage_stride;    // doubles of slice-pair staging per warp (6 n_max)
   int scratch_stride;  // doubles of Slater scratch per warp (its hot part when split)
@@ -73,6 +119,7 @@ __global__ void __launch_bounds__(kBlock) cache_prefill_kernel(PrefillParams P) 
     double* e = P.cache + s.nc_offset + ((size_t)sp * M + t) * s.nc_stride;
     const double scale = P.state[r].node_scale[sp];
     const double ep = (double)P.state[r].epoch[sp];
+    if (P.only_invalid && e[0] == ep) continue;  // warp-uniform
     // stage the species' beads of slices t (r1) and t + M/2 (r2)
     const int t2 = (t + M / 2) % M;
     __syncwarp();
@@ -127,6 +174,7 @@ struct EkPrefillParams {
   const int* slots;    // replicas to fill (null: 0 .. nslot-1)
   int nslot;
   int nslice_max;
+  const unsigned char* changed;  // [replica][nslice_max]: only these slices (null: all)
 };
 
 __global__ void __launch_bounds__(kBlock) ewald_prefill_kernel(EkPrefillParams P) {
@@ -136,6 +184,7 @@ __global__ void __launch_bounds__(kBlock) ewald_prefill_kernel(EkPrefillParams P
   const DevSys& s = P.sys[r];
   const int t = blockIdx.x;
   if (s.ek_offset < 0 || t >= s.nslice) return;
+  if (P.changed && !P.changed[(size_t)r * P.nslice_max + t]) return;
   const int np = s.npart, totk = s.totk;
   const int ky0 = s.ikmax[1], kz0 = s.ikmax[2];
   const int nx = s.ikmax[0] + 1, ny = 2 * ky0 + 1;

@@ -70,6 +70,35 @@ def test_sampler_matches_golden(pimc, case):
     assert e.thermo_energy()[0] == pytest.approx(g["energy1"], rel=1e-12)
 
 
+@pytest.mark.parametrize("case", ["dot4_fn", "heg8"])
+def test_upload_rebuilds_only_what_changed(pimc, case):
+    # pimc_upload_paths rebuilds only the cached results (Slater entries,
+    # structure factors) that depend on a changed slice.  Uploading the chain's
+    # own paths changes nothing: the chain continues bit for bit as without the
+    # upload.  Uploading paths with a few slices moved gives what an engine that
+    # rebuilt everything from those paths gives, bit for bit.
+    g = golden_io.load(case)
+    a, b, c = (engine_for(pimc, g) for _ in range(3))
+    for e in (a, b):
+        e.upload_paths([g["path0"]])
+        e.run_sections(60)
+    a.upload_paths(a.download_paths())
+    ra, rb = a.run_sections(80, records=True), b.run_sections(80, records=True)
+    for k in ("reject_level", "ipart", "ds", "ds_node", "lnt"):
+        assert np.array_equal(ra[k], rb[k]), k
+    x = a.download_paths()[0].copy()
+    rng = np.random.default_rng(11)
+    for t in rng.choice(x.shape[0], 5, replace=False):
+        x[t] += 0.02 * rng.normal(size=x[t].shape)
+    a.upload_paths([x])
+    c.set_replica_state(0, a.replica_state(0))
+    c.upload_paths([x])  # a new engine: every cached result built from x
+    ra, rc = a.run_sections(80, records=True), c.run_sections(80, records=True)
+    for k in ("reject_level", "ipart", "ds", "ds_node", "lnt"):
+        assert np.array_equal(ra[k], rc[k]), k
+    assert np.array_equal(a.download_paths()[0], c.download_paths()[0])
+
+
 def test_replicas_follow_their_own_streams(pimc):
     # Replica r of an engine reproduces the checker run with replica id r.
     g = golden_io.load("dot2_small")
