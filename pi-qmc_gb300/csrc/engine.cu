@@ -434,7 +434,7 @@ Layout make_layout(const std::vector<DevSys>& sys, int nwarps, bool& ok, LayoutO
   L.mv = take(3 * nsec);
   L.nrm = take(3 * nsec);
   L.red = take(64);
-  L.vred = take((2 * kTopLevels + 1) * kWarps);
+  L.vred = take(9 * kWarps);
   L.q = take(np);
   L.dm = take(kMaxSpecies * nsec);
   L.ndm = take(nsec);

@@ -6,13 +6,6 @@
 
 namespace pimc {
 
-// Levels proposed and evaluated together in the top-level block (L down to
-// L - kTopLevels + 1, at least level 1).  Five rather than four: at L = 5 the
-// block's 15 changed slices fill one round of config 2's 16 lane groups, and
-// config 2 and the electron gas ran 1.6 % and 1.8 % faster per launch (the
-// uneven batch 2 % slower).
-constexpr int kTopLevels = 5;
-
 // Offsets (in doubles) of the shared-memory working set; computed on the host
 // for the largest replica of a launch.
 struct Layout {
@@ -704,15 +697,13 @@ static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, d
                                   double* llt, double* lnd) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const int nsec = s.nsec, nsm = s.ns_max, L = s.nlevel;
-  // hi - lo + 1 <= kTopLevels levels: v[0..kTopLevels) mover terms, then the action terms
-  double v[2 * kTopLevels];
-#pragma unroll
-  for (int k = 0; k < 2 * kTopLevels; ++k) v[k] = 0.0;
+  // hi - lo + 1 <= 4 levels: v[0..3] mover terms, v[4..7] action terms
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int level = hi; level >= lo; --level) {
     const double p = mover_level_part(s, m, ipart, level, seed, s.stream_id, att,
                                       level_uniform_base(s, level));
 #pragma unroll
-    for (int k = 0; k < kTopLevels; ++k)
+    for (int k = 0; k < 4; ++k)
       if (k == hi - level) v[k] = p;
     __syncthreads();  // this level's beads before the next level's midpoints
   }
@@ -786,17 +777,17 @@ static __device__ __noinline__ void top_levels(const DevSys& s, const Smem& m, d
     for (int level = lo; level <= hi; ++level) {
       const double a = action_partial(s, m, ipart, level, threadIdx.x - a0, blockDim.x - a0);
 #pragma unroll
-      for (int k = 0; k < kTopLevels; ++k)
-        if (k == level - lo) v[kTopLevels + k] = a;
+      for (int k = 0; k < 4; ++k)
+        if (k == level - lo) v[4 + k] = a;
     }
   __syncthreads();
   const int flags = m.ictl[C_FLAG];
-  double* out = m.vred + 2 * kTopLevels * kWarps;
-  block_sum_vec(v, 2 * kTopLevels, m.vred, out);
+  double* out = m.vred + 8 * kWarps;
+  block_sum_vec(v, 8, m.vred, out);
   if (threadIdx.x == 0)
     for (int level = lo; level <= hi; ++level) {
       llt[level] = out[hi - level];
-      lds[level] = out[kTopLevels + level - lo];
+      lds[level] = out[4 + level - lo];
       lnd[level] = ((flags >> level) & 1) ? 2e100 : 0.0;
     }
   __syncthreads();
@@ -998,7 +989,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       // discarded.
       // (with delayed rejection every level is taken in turn: a second proposal
       // at level L - 1 changes the normals and uniforms of the levels under it)
-      const int lb = (L >= 2 && !s.dr) ? max(1, L - kTopLevels + 1) : L + 1;
+      const int lb = (L >= 2 && !s.dr) ? max(1, L - 3) : L + 1;
       if (lb <= L) {
         double* lds = m.red + kWarps + 8;  // [kMaxLevels] per level: action difference,
         double* llt = lds + kMaxLevels;     // mover ln T,
