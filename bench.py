@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=600,
                    help="requests of the serving sub-run in the default line (0: none)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--other-configs", default="dot2,heg54,batch4096",
+                   help="workloads measured in short sub-runs of the default line ('' : none)")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     p.add_argument("--launch", default="",
                    help="block,scratch_global,regs_variant: this launch shape, no autotuning")
@@ -790,6 +792,38 @@ def section_roofline(args, systems, batch, kw, R, A, reach, depth_reach, section
     return out
 
 
+# ---------------------------------------------------------------- other configs
+def other_config_subrun(args, name):
+    """A short run of another workload of the hot path (3 warm-up and 3 timed
+    steps, its own equilibration and autotuned launch shape), reported
+    compactly beside the headline: the same measurement as its own line."""
+    sub = argparse.Namespace(**vars(args))
+    sub.workload = name
+    sub.precision = workload_precision(name, "auto")
+    sub.steps, sub.warmup = 3, 3
+    sub.replicas = sub.attempts = 0
+    sub.equil = -1
+    sub.launch = ""
+    out = run_engine(sub, 0, 1)
+    r = out["roofline"]
+    e = out["energy"]
+    keep = {"value": out["value"], "unit": out["unit"], "e2e": out["e2e"]["value"],
+            "ms_per_step": out["ms_per_step"], "steps": sub.steps, "warmup": sub.warmup,
+            "dtype": out["dtype"], "workload": out["config"]["workload"],
+            "replicas": out["config"]["replicas_per_gpu"],
+            "attempts_per_replica_per_step": out["config"]["attempts_per_replica_per_step"],
+            "launch": out["launch"]["chosen"], "gpu_launches": out["gpu_launches"],
+            "clocks": out["clocks"],
+            "roofline": {k: r.get(k) for k in ("bound", "achieved", "peak", "unit", "frac",
+                                              "traffic", "section_ms_per_launch",
+                                              "count_stale")},
+            "energy": {k: e.get(k) for k in ("value", "stat_err", "reference",
+                                             "diff_over_sigma", "within_2sigma_of_reference")}}
+    if "batched_over_plain" in out:
+        keep["batched_over_plain"] = out["batched_over_plain"]
+    return keep
+
+
 # ---------------------------------------------------------------- serving sub-run
 def serving_subrun(args):
     """A short run of the serving stream (config 5's distributions and arrival
@@ -880,6 +914,11 @@ def main():
     if rank == 0 and world == 1:
         if args.workload != "serve" and args.serve_requests > 0:
             out["serving"] = serving_subrun(args)
+        if args.workload == "dot20_fn" and args.other_configs:
+            # configs 1, 3 and 4 of the hot path, each measured as its own line
+            # would be (`--workload <name>`), in short form
+            out["other_configs"] = {w: other_config_subrun(args, w)
+                                    for w in args.other_configs.split(",") if w}
         if not args.no_cpu_baseline:
             kws, batch, R, kw, A = engine_setup(args)
             out["cpu_baseline"] = cpu_baseline(kws, A, args.cpu_seconds, os.cpu_count() or 1)
