@@ -1621,8 +1621,13 @@ int64_t pimc_kernel_launches(pimc_engine* e) { return e ? e->launches : 0; }
 namespace {
 int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int minb) {
   if (minb < 1 || minb > 4) return fail(PIMC_ERR_INVALID, "register variant must be 1, 2, 3 or 4");
-  if (block != 64 && block != 128 && block != 256 && !(block == 512 && minb == 1))
-    return fail(PIMC_ERR_INVALID, "block must be 64, 128, 256 (or 512 with variant 1)");
+  bool fixed = false;
+  for (const DevSys& d : e->hsys) fixed |= d.fixed_node != 0;
+  // one warp per replica (block 32) only for systems without node models
+  if (block != 64 && block != 128 && block != 256 && !(block == 512 && minb == 1) &&
+      !(block == 32 && !fixed && minb >= 2))
+    return fail(PIMC_ERR_INVALID,
+                "block must be 64, 128, 256 (512 with variant 1, 32 without node models)");
   bool ok = false;
   const Layout L = make_layout(e->hsys, block / 32, ok, opts);
   if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
@@ -1727,8 +1732,9 @@ int pimc_engine_autotune(pimc_engine* e, int nattempt, pimc_launch_config* best,
   for (const DevSys& d : e->hsys) fixed |= d.fixed_node != 0;
   std::vector<pimc_launch_config> cand;
   for (int v : {2, 3, 4})
-    for (int b : {64, 128, 256})
-      for (int g = 0; g < (fixed ? 3 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
+    for (int b : {32, 64, 128, 256})
+      if (b > 32 || !fixed)
+        for (int g = 0; g < (fixed ? 3 : 1); ++g) cand.push_back({b, g, 0, v, 0.f});
   for (int g = 0; g < (fixed ? 3 : 1); ++g) cand.push_back({512, g, 0, 1, 0.f});
   cudaEvent_t t0, t1;
   CU(cudaEventCreate(&t0));

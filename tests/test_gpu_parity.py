@@ -418,6 +418,33 @@ def test_electron_gas_scratch_placements(pimc, block, scratch_global, regs):
     assert np.abs(e.download_paths()[0] - g["path1"]).max() <= 1e-12
 
 
+@pytest.mark.parametrize("case", ["dot2_small", "dot2_dr", "dot3_prim"])
+@pytest.mark.parametrize("regs", [2, 4])
+def test_one_warp_per_replica_matches_golden(pimc, case, regs):
+    # Systems without node models may run one warp per replica (32-thread
+    # blocks): pi-qmc's decisions, action differences and path all the same.
+    g = golden_io.load(case)
+    e = engine_for(pimc, g)
+    e.configure(32, 0, 0, regs)
+    assert e.launch_config()["block"] == 32
+    e.upload_paths([g["path0"]])
+    rec = e.run_sections(g["nattempt"], records=True)
+    ref = g["records"]
+    for k in ("ifirst1", "ipart", "reject_level"):
+        assert np.array_equal(rec[k][0], ref[k]), k
+    nl = g["kw"]["nlevel"] + 1
+    assert rel_close(rec["ds"][0][:, :nl], ref["ds"][:, :nl], 1e-12)
+    assert rel_close(rec["lnt"][0][:, :nl], ref["lnt"][:, :nl], 1e-12)
+    assert np.abs(e.download_paths()[0] - g["path1"]).max() <= 1e-12
+
+
+def test_one_warp_blocks_refused_with_node_models(pimc):
+    g = golden_io.load("dot4_fn")
+    e = engine_for(pimc, g)
+    with pytest.raises(pimc.PimcError):
+        e.configure(32, 0, 0, 2)
+
+
 def test_autotune_does_not_advance_chains(pimc):
     g = golden_io.load("dot4_fn")
     a = engine_for(pimc, g, nreplica=8)
