@@ -1,7 +1,7 @@
 // The bisection section-move kernel: one CTA advances one replica through a
 // sequence of section-move attempts, entirely on the device.
 //
-// Per attempt (pi-qmc order, SURVEY call stacks CS1/CS2):
+// Per attempt (pi-qmc order: SectionChooser.cc:30-48, DoubleSectionChooser.cc:33-65):
 //   SectionChooser::run / DoubleSectionChooser::run   -> choose section(s), stage in smem
 //   FixedNodeAction::initialize                        -> det + distances on every slice
 //   SimpleParticleChooser::chooseParticles             -> moving particle
