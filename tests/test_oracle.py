@@ -134,6 +134,35 @@ def test_port_matches_reference_dot(seed):
 
 
 @needs_ref
+@pytest.mark.parametrize("factors", [(0.0, 0.0), (0.8, 0.5), (1.4, 1.1)])
+@pytest.mark.parametrize("fixed", [False, True])
+def test_port_matches_reference_delayed_rejection(factors, fixed):
+    # Delayed rejection (MultiLevelSampler / DoubleMLSampler with the
+    # FreeMover) at pi-qmc's default and at other sigma factors, the
+    # restatement against pi-qmc's own code on the same streams.
+    sf, nf = factors
+    if fixed:
+        kw = W.dot20_fn(counts=[2, 2], nslice=64, beta=4.0, nlevel=3, seed=21)
+        init = "const"
+    else:
+        kw = W.dot2(nslice=64, seed=21)
+        init = "gauss"
+    kw = dict(kw, delayed_rejection=1, sigma_factor=sf, dr_sigma_factor=nf)
+    cfg = O.make_config(**kw)
+    ref = O.RefOracle(cfg)
+    port = O.PortOracle(cfg, ref.pair_tables(), ref.ewald_table())
+    x = W.initial_path(cfg, init, seed=21)
+    ref.set_path(x)
+    port.set_path(x)
+    a, b = ref.run(300), port.run(300)
+    for k in ("ifirst1", "ipart", "reject_level"):
+        assert np.array_equal(a[k], b[k]), k
+    assert rel_close(a["ds"], b["ds"], 1e-12)
+    assert rel_close(a["lnt"], b["lnt"], 1e-12)
+    assert np.abs(ref.get_path() - port.get_path()).max() <= 1e-12
+
+
+@needs_ref
 def test_port_matches_reference_action_levels():
     # Action-level parity at every level on random sections (FakeSampler).
     kw = W.dot20_fn(counts=[3, 2], nslice=64, nlevel=4, node_kind=[0, 0])
