@@ -32,6 +32,16 @@ void section_smem_cap_v1(int);
 void section_smem_cap_v2(int);
 void section_smem_cap_v3(int);
 void section_smem_cap_v4(int);
+// the same without the fixed-node phases (launches without node models)
+cudaError_t section_launch_nf_v2(int, int, size_t, cudaStream_t, const RunParams&);
+cudaError_t section_launch_nf_v3(int, int, size_t, cudaStream_t, const RunParams&);
+cudaError_t section_launch_nf_v4(int, int, size_t, cudaStream_t, const RunParams&);
+int section_occupancy_nf_v2(int, size_t);
+int section_occupancy_nf_v3(int, size_t);
+int section_occupancy_nf_v4(int, size_t);
+void section_smem_cap_nf_v2(int);
+void section_smem_cap_nf_v3(int);
+void section_smem_cap_nf_v4(int);
 }  // namespace pimc
 
 using namespace pimc;
@@ -39,15 +49,27 @@ using namespace pimc;
 namespace {
 // minb: 2, 3 or 4 resident 256-thread blocks per SM worth of registers, or 1:
 // the 512-thread variant (128 registers)
+// nodes: whether a system of the launch has a node model (else the variant
+// without the fixed-node phases runs; the 512-thread variant has none)
 cudaError_t section_launch(int minb, int grid, int block, size_t smem, cudaStream_t st,
-                           const RunParams& P) {
+                           const RunParams& P, bool nodes = true) {
   if (minb == 1) return section_launch_v1(grid, block, smem, st, P);
+  if (!nodes) {
+    if (minb == 3) return section_launch_nf_v3(grid, block, smem, st, P);
+    if (minb == 4) return section_launch_nf_v4(grid, block, smem, st, P);
+    return section_launch_nf_v2(grid, block, smem, st, P);
+  }
   if (minb == 3) return section_launch_v3(grid, block, smem, st, P);
   if (minb == 4) return section_launch_v4(grid, block, smem, st, P);
   return section_launch_v2(grid, block, smem, st, P);
 }
-int section_occupancy(int minb, int block, size_t smem) {
+int section_occupancy(int minb, int block, size_t smem, bool nodes = true) {
   if (minb == 1) return section_occupancy_v1(block, smem);
+  if (!nodes) {
+    if (minb == 3) return section_occupancy_nf_v3(block, smem);
+    if (minb == 4) return section_occupancy_nf_v4(block, smem);
+    return section_occupancy_nf_v2(block, smem);
+  }
   if (minb == 3) return section_occupancy_v3(block, smem);
   if (minb == 4) return section_occupancy_v4(block, smem);
   return section_occupancy_v2(block, smem);
@@ -127,6 +149,7 @@ struct pimc_engine {
   DevBuf<long long> d_ekcache;  // structure factors per replica and slice
   DevBuf<long long> d_ekstage;  // per-CTA staging of an attempt's new structure factors
   int ekstage_stride = 0;       // int64 words per CTA
+  bool nodes = true;            // a system with a node model (else the kernels without them run)
   DevBuf<double> d_upload;      // pimc_upload_paths: the host paths, before comparison
   DevBuf<unsigned char> d_changed;  // [replica][nslice_max]: slices the upload changed
   DevBuf<double> d_xstage;      // mixed form: per-CTA staging of changed slices' inverses
@@ -512,6 +535,9 @@ void set_smem_caps() {
   section_smem_cap_v2(kSmemLimit);
   section_smem_cap_v3(kSmemLimit);
   section_smem_cap_v4(kSmemLimit);
+  section_smem_cap_nf_v2(kSmemLimit);
+  section_smem_cap_nf_v3(kSmemLimit);
+  section_smem_cap_nf_v4(kSmemLimit);
   cudaFuncSetAttribute(thermo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
   cudaFuncSetAttribute(action_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kSmemLimit);
@@ -676,6 +702,8 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
     e->block = fixed ? kBlock : (items <= 64 ? 64 : (items <= 128 ? 128 : kBlock));
   }
   for (DevSys& d : e->hsys) d.mixed = precision == PIMC_PREC_MIXED;
+  e->nodes = false;
+  for (const DevSys& d : e->hsys) e->nodes |= d.fixed_node != 0;
   bool ok = false;
   e->lay = make_layout(e->hsys, e->block / 32, ok);
   if (!ok) {
@@ -716,7 +744,7 @@ int build_engine(const pimc_system* sys, int nrep, const pimc_pair_table* tables
   // shared by all engines of the process).
   set_smem_caps();
   int occ = 1;
-  occ = section_occupancy(e->minb, e->block, e->lay.total * 8);
+  occ = section_occupancy(e->minb, e->block, e->lay.total * 8, e->nodes);
   occ = std::max(occ, 1);
   e->grid = std::min(nrep, nsm * occ);
   for (DevSys& d : e->hsys) d.inv_offset = e->lay.gcta > 0 ? 0 : -1;
@@ -1184,7 +1212,7 @@ int pimc_run_sections(pimc_engine* e, int nattempt, pimc_move_record* records) {
   RunParams P;
   fill_run_params(e, P, nattempt, d_rec);
   CU(cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->stream));
-  CU(section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->stream, P));
+  CU(section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->stream, P, e->nodes));
   e->launches++;
   if (records) {
     CU(cudaMemcpyAsync(records, d_rec, sizeof(pimc_move_record) * (size_t)e->nrep * nattempt,
@@ -1423,7 +1451,7 @@ int pimc_run_steps(pimc_engine* e, int nattempt, int nsteps, double* host_energy
         RunParams P;
         fill_run_params(e, P, nattempt, nullptr);
         cudaMemsetAsync(e->d_next.p, 0, sizeof(int), e->cap_stream);
-        section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->cap_stream, P);
+        section_launch(e->minb, e->grid, e->block, e->lay.total * 8, e->cap_stream, P, e->nodes);
       }
       rc = enqueue_thermo(e, e->cap_stream, k);
     }
@@ -1632,7 +1660,7 @@ int apply_config(pimc_engine* e, int block, LayoutOpts opts, int ctas_cap, int m
   const Layout L = make_layout(e->hsys, block / 32, ok, opts);
   if (!ok) return fail(PIMC_ERR_CAPACITY, "working set does not fit in shared memory");
   int occ = 1;
-  occ = section_occupancy(minb, block, L.total * 8);
+  occ = section_occupancy(minb, block, L.total * 8, e->nodes);
   occ = std::max(occ, 1);
   if (ctas_cap > 0) occ = std::min(occ, ctas_cap);
   const int grid = std::min(e->nrep, e->num_sms * occ);

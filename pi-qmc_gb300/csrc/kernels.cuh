@@ -889,7 +889,10 @@ static __device__ __noinline__ void delayed_rejection(const DevSys& s, const Sme
 // NT (largest block) and MINB set the register budget, 65536 / (NT * MINB)
 // per thread; the variants are compiled in separate translation units
 // (section_variants.cu) and chosen at run time by the launch configuration.
-template <int NT, int MINB>
+// kNodes = false: the variant for launches without node models, whose code
+// leaves the fixed-node phases out (a smaller kernel: fewer instruction-fetch
+// stalls when thousands of one-warp CTAs run different phases).
+template <int NT, int MINB, bool kNodes = true>
 __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
   extern __shared__ double smem[];
   __shared__ DevSys S;
@@ -936,6 +939,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
     long long* ek = (P.ekcache && s.ek_offset >= 0) ? P.ekcache + s.ek_offset : nullptr;
     long long* ekstage = ek ? P.ekstage + (size_t)blockIdx.x * P.ekstage_stride : nullptr;
     const int np = s.npart, nsec = s.nsec, M = s.nslice, L = s.nlevel;
+    const bool fixed = kNodes && s.fixed_node;
     for (int i = threadIdx.x; i < np; i += blockDim.x) m.qpart[i] = s.charge[species_of(s, i)];
     const int nat = P.nattempt_r ? P.nattempt_r[r] : P.nattempt;
     for (int a = 0; a < nat; ++a) {
@@ -945,7 +949,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         int i1, i2 = -2;
         uint32_t ui = 0;
         const double x = stream_uniform(P.seed, s.stream_id, att, ui++) * (1 - 1e-8);
-        if (!s.fixed_node) {
+        if (!fixed) {
           const int ilo = -1, ihi = M - 1;
           i1 = ilo + (int)((ihi + 1 - ilo) * x);
           if (i1 > ihi) i1 = ihi;
@@ -967,7 +971,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       const int ifirst1 = m.ictl[C_IFIRST1], ifirst2 = m.ictl[C_IFIRST2];
       const int ipart = m.ictl[C_IPART];
       load_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
-      if (s.fixed_node) load_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+      if (fixed) load_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
       attempt_normals(s, m, P.seed, s.stream_id, att);
       __syncthreads();
       for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
@@ -976,8 +980,8 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         m.mz[t] = m.s1z[t * np + ipart];
       }
       const int msp = species_of(s, ipart);
-      const bool mynode = s.fixed_node && s.node_kind[msp];
-      if (s.fixed_node)
+      const bool mynode = fixed && s.node_kind[msp];
+      if (fixed)
         node_initialize(s, m, scale, epoch, mynode ? msp : -1, &status, cache, ifirst1);
       __syncthreads();
       pimc_move_record* rec = P.rec ? P.rec + (size_t)r * P.nattempt + a : nullptr;
@@ -1011,9 +1015,9 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
             ds = lds[level];
             dsn = lnd[level];
             lnT = llt[level];
-            total = s.fixed_node ? ds + dsn : ds;
+            total = fixed ? ds + dsn : ds;
             const double old =
-                level == L ? 0.0 : (s.fixed_node ? lds[level + 1] + lnd[level + 1] : lds[level + 1]);
+                level == L ? 0.0 : (fixed ? lds[level + 1] + lnd[level + 1] : lds[level + 1]);
             const uint32_t ubase = level_uniform_base(s, level);
             const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
             const uint32_t uacc = ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
@@ -1055,7 +1059,7 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         double dsn = 0.0;
         if (mynode) dsn = node_level(s, m, scale[msp], msp, ipart, level, cache, ifirst1, epoch[msp]);
         if (threadIdx.x == 0) {
-          const double total = s.fixed_node ? ds + dsn : ds;
+          const double total = fixed ? ds + dsn : ds;
           const uint32_t nmov = (level == L) ? 0u : (1u << (L - level - 1));
           const uint32_t uacc =
               ubase + (s.mover == PIMC_MOVER_FREE_PBC ? 3u * nmov : 0u);
@@ -1149,9 +1153,9 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
       }
       __syncthreads();
       // SerialPaths::putDoubleBeads order (src/base/SerialPaths.cc:187-205).
-      if (!s.fixed_node || ifirst1 < M / 2 - 1) {
+      if (!fixed || ifirst1 < M / 2 - 1) {
         store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
-        if (s.fixed_node) {
+        if (fixed) {
           __syncthreads();
           store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
         }

@@ -15,7 +15,10 @@ LIB = os.path.join(PKG, "libpimc_gb300.so")
 # separate objects so that nvcc compiles them in parallel
 SOURCES = [("engine.cu", []), ("tables.cc", []), ("paths_io.cc", [])] + [
     ("section_variants.cu", [f"-DPIMC_NT={nt}", f"-DPIMC_MINB={v}"])
-    for nt, v in ((256, 2), (256, 3), (256, 4), (512, 1))]
+    for nt, v in ((256, 2), (256, 3), (256, 4), (512, 1))] + [
+    # the variants without the fixed-node phases (launches without node models)
+    ("section_variants.cu", ["-DPIMC_NT=256", f"-DPIMC_MINB={v}", "-DPIMC_NODES=0"])
+    for v in (2, 3, 4)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
