@@ -121,17 +121,17 @@ def sweep_attempts(kw):
 MEASURED_WORK = {
     # launch shape of the count (block, scratch placement, register variant):
     # the DRAM bytes depend on the scratch placement, the flops do not
-    ("dot20_fn", "mixed"): dict(fp64=3.220e5, fp32=1.895e5, dram=1.471e5, shape="256,0,2",
-                                sha="f6358756d5cbaad2"),
-    ("dot20_fn", "fp64"): dict(fp64=6.504e5, fp32=4.475e3, dram=1.439e5, shape="256,0,2",
-                               sha="f6358756d5cbaad2"),
+    ("dot20_fn", "mixed"): dict(fp64=3.220e5, fp32=1.895e5, dram=1.481e5, shape="256,0,2",
+                                sha="159f1ae6eddc1bff"),
+    ("dot20_fn", "fp64"): dict(fp64=6.504e5, fp32=4.475e3, dram=1.551e5, shape="256,2,2",
+                               sha="159f1ae6eddc1bff"),
     # counted on the first 1024 replicas of the mix
-    ("batch4096", "mixed"): dict(fp64=1.474e5, fp32=8.393e4, dram=4.637e4, shape="128,2,2",
-                                 sha="f6358756d5cbaad2"),
-    ("heg54", "mixed"): dict(fp64=1.891e6, fp32=5.344e5, dram=4.014e6, shape="512,2,1",
-                             sha="f6358756d5cbaad2"),
-    ("dot2", "fp64"): dict(fp64=1.945e4, fp32=164.4, dram=6.335e3, shape="64,0,4",
-                           sha="f6358756d5cbaad2"),
+    ("batch4096", "mixed"): dict(fp64=1.474e5, fp32=8.393e4, dram=4.632e4, shape="128,2,2",
+                                 sha="159f1ae6eddc1bff"),
+    ("heg54", "mixed"): dict(fp64=1.891e6, fp32=5.344e5, dram=4.020e6, shape="512,2,1",
+                             sha="159f1ae6eddc1bff"),
+    ("dot2", "fp64"): dict(fp64=1.760e4, fp32=164.4, dram=496.9, shape="32,0,2",
+                           sha="159f1ae6eddc1bff"),
 }
 
 
