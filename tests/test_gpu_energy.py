@@ -98,3 +98,19 @@ def test_energy_matches_pi_qmc(pimc, case, kind, equil, measure, precision):
     assert ref["block_means"].size >= 50
     assert abs(e - er) <= 2 * math.hypot(sig, sr), (case, precision, e, sig, er, sr)
     assert sig <= 0.01 * abs(er)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_delayed_rejection_energy(pimc, precision):
+    # Delayed rejection changes the proposals, not the target: config 1's dot
+    # with pi-qmc's delayedRejection (default factors: 1 and newSigmaFactor
+    # 0.75) reproduces pi-qmc's equilibrated energy of the same system without
+    # it (tests/golden/energy_dot2_full.npz), same protocol, within 2 sigma.
+    ref = np.load(golden_io.GOLDEN + "/energy_dot2_full.npz")
+    g = golden_io.load("dot2_full")
+    kw = dict(g["kw"], delayed_rejection=1)
+    e, sig = equilibrated_energy(pimc, kw, g["tables"], "gauss", precision, 512, 500, 600,
+                                 sweep_attempts(kw), disp=int(ref["disp"]))
+    er, sr = float(ref["energy"]), float(ref["sigma"])
+    assert abs(e - er) <= 2 * math.hypot(sig, sr), (precision, e, sig, er, sr)
+
