@@ -998,8 +998,25 @@ int pimc_upload_paths(pimc_engine* e, const double* host_xyz) {
   if (e->d_upload.n < n || e->d_changed.n < nflag) {
     CU(cudaStreamSynchronize(e->stream));
     if ((e->d_upload.n < n && e->d_upload.alloc(n)) ||
-        (e->d_changed.n < nflag && e->d_changed.alloc(nflag)))
-      return fail(PIMC_ERR_CUDA, "cudaMalloc upload staging");
+        (e->d_changed.n < nflag && e->d_changed.alloc(nflag))) {
+      // no room for the staging copy: copy in place and rebuild every cache
+      cudaGetLastError();  // (the failed allocation's error is handled here)
+      e->d_upload.free();
+      e->d_changed.free();
+      CU(cudaMemcpyAsync(e->d_paths.p, host_xyz, n * sizeof(double), cudaMemcpyHostToDevice,
+                         e->stream));
+      const dim3 grid(16, (unsigned)std::min(e->nrep, 65535));
+      path_scan_kernel<<<grid, kBlock, 0, e->stream>>>(e->d_sys.p, e->d_state.p, e->d_paths.p,
+                                                       e->nrep);
+      CU(cudaGetLastError());
+      e->launches++;
+      if (e->d_nodecache.p) {
+        CU(cudaMemsetAsync(e->d_nodecache.p, 0xff, e->d_nodecache.n * sizeof(double),
+                           e->stream));
+        if (int rc = prefill_cache(e, e->d_nodecache.p, nullptr, e->nrep)) return rc;
+      }
+      return prefill_ewald(e, nullptr, e->nrep);
+    }
   }
   CU(cudaMemcpyAsync(e->d_upload.p, host_xyz, n * sizeof(double), cudaMemcpyHostToDevice,
                      e->stream));
