@@ -1152,17 +1152,32 @@ __global__ void __launch_bounds__(NT, MINB) section_moves_kernel(RunParams P) {
         rec->reject_level = reject;
       }
       __syncthreads();
-      // SerialPaths::putDoubleBeads order (src/base/SerialPaths.cc:187-205).
-      if (!fixed || ifirst1 < M / 2 - 1) {
-        store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
-        if (fixed) {
+      // SerialPaths::putBeads / putDoubleBeads (src/base/SerialPaths.cc:143-205).
+      // The sections come back unchanged but for the moving particle's interior
+      // beads of section 1 when the move was accepted, so only those are
+      // written, unless the two sections overlap beyond their end slices
+      // (2^L > M/2), where pi-qmc's put order decides which copy a shared
+      // slice keeps and both sections are written in that order.
+      if (fixed && (1 << L) > M / 2) {
+        if (ifirst1 < M / 2 - 1) {
+          store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
           __syncthreads();
           store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+        } else {
+          store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
+          __syncthreads();
+          store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
         }
-      } else {
-        store_section(s, path, ifirst2, m.s2x, m.s2y, m.s2z);
-        __syncthreads();
-        store_section(s, path, ifirst1, m.s1x, m.s1y, m.s1z);
+      } else if (reject < 0) {
+        for (int k = 1 + threadIdx.x; k < nsec - 1; k += blockDim.x) {
+          const int islice = ifirst1 + k;
+          if (islice < 0) continue;
+          const int t = islice < M ? islice : islice % M;
+          double* dst = path + ((size_t)t * np + ipart) * 3;
+          dst[0] = m.s1x[k * np + ipart];
+          dst[1] = m.s1y[k * np + ipart];
+          dst[2] = m.s1z[k * np + ipart];
+        }
       }
       __syncthreads();
     }
