@@ -121,17 +121,17 @@ def sweep_attempts(kw):
 MEASURED_WORK = {
     # launch shape of the count (block, scratch placement, register variant):
     # the DRAM bytes depend on the scratch placement, the flops do not
-    ("dot20_fn", "mixed"): dict(fp64=3.220e5, fp32=1.895e5, dram=1.481e5, shape="256,0,2",
-                                sha="159f1ae6eddc1bff"),
-    ("dot20_fn", "fp64"): dict(fp64=6.504e5, fp32=4.475e3, dram=1.551e5, shape="256,2,2",
-                               sha="159f1ae6eddc1bff"),
+    ("dot20_fn", "mixed"): dict(fp64=3.220e5, fp32=1.895e5, dram=1.082e5, shape="256,0,2",
+                                sha="6f18248147df49dd"),
+    ("dot20_fn", "fp64"): dict(fp64=6.504e5, fp32=4.475e3, dram=1.141e5, shape="256,2,2",
+                               sha="6f18248147df49dd"),
     # counted on the first 1024 replicas of the mix
-    ("batch4096", "mixed"): dict(fp64=1.474e5, fp32=8.393e4, dram=4.632e4, shape="128,2,2",
-                                 sha="159f1ae6eddc1bff"),
-    ("heg54", "mixed"): dict(fp64=1.891e6, fp32=5.344e5, dram=4.020e6, shape="512,2,1",
-                             sha="159f1ae6eddc1bff"),
-    ("dot2", "fp64"): dict(fp64=1.760e4, fp32=164.4, dram=496.9, shape="32,0,2",
-                           sha="159f1ae6eddc1bff"),
+    ("batch4096", "mixed"): dict(fp64=1.474e5, fp32=8.393e4, dram=3.358e4, shape="128,2,2",
+                                 sha="6f18248147df49dd"),
+    ("heg54", "mixed"): dict(fp64=1.891e6, fp32=5.344e5, dram=3.924e6, shape="512,1,1",
+                             sha="6f18248147df49dd"),
+    ("dot2", "fp64"): dict(fp64=1.760e4, fp32=164.4, dram=558.3, shape="32,0,3",
+                           sha="6f18248147df49dd"),
 }
 
 
