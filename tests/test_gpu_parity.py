@@ -453,7 +453,9 @@ def test_autotune_does_not_advance_chains(pimc):
         e.upload_paths([g["path0"]] * 8)
     best, tried = a.autotune(8)
     assert len(tried) >= 3 and all(t["ms"] != 0 for t in tried)
-    assert best["ms"] > 0 and best["ms"] == min(t["ms"] for t in tried if t["ms"] > 0)
+    # the choice is one of the three fastest short trials (re-timed on longer ones)
+    fastest = sorted((t for t in tried if t["ms"] > 0), key=lambda t: t["ms"])[:3]
+    assert best["ms"] > 0 and any(t == best for t in fastest), (best, fastest)
     acc, att, st = a.replica_status()
     assert att.sum() == 0
     # the engine runs the shape the tuner reports (scratch placement included)
