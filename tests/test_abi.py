@@ -44,3 +44,45 @@ def test_errors_without_an_engine(lib):
     assert lib.pimc_last_error()
     assert lib.pimc_write_paths(None, 0, b"x") == -1
     assert lib.pimc_paths_write_file(None, None, 1, 1) == -1
+
+
+# C struct <-> ctypes Structure of the Python binding
+STRUCTS = {"pimc_system": "System", "pimc_pair_table": "PairTable",
+           "pimc_ewald_table": "EwaldTable", "pimc_move_record": "MoveRecord",
+           "pimc_replica_state": "ReplicaState", "pimc_displace_record": "DisplaceRecord",
+           "pimc_launch_config": "LaunchConfig", "pimc_server_config": "ServerConfig"}
+
+
+def test_binding_structs_match_the_header(tmp_path):
+    # Every structure the Python binding passes through the ABI has the C
+    # header's size and field offsets (compiled with the host C compiler).
+    import shutil
+    import subprocess
+    import pimc_gb300
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"',
+             "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(pimc_gb300, pyname)
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            a, b, v = line.split()
+            got[(a, b)] = int(v)
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(pimc_gb300, pyname)
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+
