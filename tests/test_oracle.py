@@ -2,6 +2,7 @@
 own unit-test known answers, the golden fixtures made by pi-qmc's own code,
 and (where the reference tree is present) oracle/_ref directly."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -282,3 +283,39 @@ def test_node_fixtures_exercise_the_nodal_action():
         for ref in golden_io.load_nodes(case)["species"].values():
             assert np.all(ref["det"] != 0) and np.all(np.isfinite(ref["d1"]))
             assert np.any(ref["d1"] < 200) and np.any(ref["d2"] < 200)
+
+
+def test_oracle_structs_match_the_header(tmp_path):
+    # The ctypes structures of oracle_lib have oracle_api.h's layouts.
+    import ctypes as C
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    hdr = os.path.join(os.path.dirname(O.__file__), "oracle_api.h")
+    structs = {"ora_config": O.OraConfig, "ora_record": O.OraRecord,
+               "ora_drecord": O.OraDRecord, "ora_pair_table": O.OraPairTable,
+               "ora_ewald_table": O.OraEwaldTable}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", "#include <stdint.h>",
+             f'#include "{hdr}"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                               check=True).stdout.split("\n"):
+        if line:
+            a, b, v = line.split()
+            got[(a, b)] = int(v)
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+
